@@ -1,0 +1,409 @@
+"""Benchmark: tiled SpGEMM GFLOP/s and HBM-roofline fraction on one GB300.
+
+Default workload: C = A*A, A = R-MAT scale 20 (n = 2^20, 16 edges per vertex
+before merging, (a,b,c,d) = (.57,.19,.19,.05), duplicates merged), FP32 values
+U[-1,1] -- the configuration the metric is quoted on.  A "step" is one full
+SpGEMM (C tile structure + bitmask symbolic + numeric, with every allocation
+of C) on tiles already resident in HBM; GFLOP/s = 2 * products / step time,
+products = sum over A's nonzeros of nnz(B row) (src/spgemm_raw_v2.cu:95-99,250).
+
+Printed JSON (rank 0, one line) carries:
+  value      GFLOP/s of the device-resident steps (max over ranks of the time)
+  e2e        the same metric through the public C ABI with host buffers: each
+             step copies the CSR inputs host->device, tiles them, multiplies and
+             copies every array of C back to pinned host memory
+  roofline   the dominant kernel's algorithmic bytes / its CUDA-event time
+  cpu_baseline  OpenMP Gustavson (the CPU oracle's port of the reference's
+             check, src/spgemm_raw_v2.cu:289-338) on a seeded row sample
+
+`--impl reference` times the reference's CPU implementation of the path (that
+Gustavson port) on all host threads for the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from gpu_spgemm_gb300 import synth  # noqa: E402
+
+L2_BYTES = 129 * 1024 * 1024
+TS = 16
+
+
+def workload(name: str):
+    if name == "rmat20":
+        a = synth.rmat(20, 16)
+        return a, a, {"workload": "C=A*A, A=R-MAT scale 20, edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), "
+                                  "duplicates merged, FP32 U[-1,1]", "n": a.m, "nnz": a.nnz}
+    if name == "poisson2d":
+        a = synth.poisson2d(256)
+        return a, a, {"workload": "C=A*A, A=2-D 5-point Poisson 256x256, FP64", "n": a.m, "nnz": a.nnz}
+    if name == "stencil27":
+        a = synth.stencil27_dof3(64)
+        return a, a, {"workload": "C=A*A, A=27-point stencil 64^3 x 3 dof, FP32 N(0,1)", "n": a.m, "nnz": a.nnz}
+    if name.startswith("rmat"):
+        s = int(name[4:])
+        a = synth.rmat(s, 16)
+        return a, a, {"workload": f"C=A*A, A=R-MAT scale {s}, edge factor 16, FP32", "n": a.m, "nnz": a.nnz}
+    raise SystemExit(f"unknown workload {name}")
+
+
+def tile_bytes(numtile, nnz, tilem, v, b_side=False):
+    """Compulsory bytes of one tile matrix: tile_ptr, per tile colidx + nnz
+    prefix + 16 row offsets + 16 row masks, per nonzero value + column byte;
+    B additionally its CSC tile pointer/rowidx arrays."""
+    b = 4 * (tilem + 1) + numtile * (4 + 4 + 16 + 32) + nnz * (v + 1)
+    if b_side:
+        b += 4 * (tilem + 1) + 4 * numtile
+    return b
+
+
+def c_bytes(numtileC, nnzC, tilem, v):
+    return 4 * (tilem + 1) + numtileC * (4 + 4 + 8 + 32 + 16) + nnzC * (v + 1)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, flag in zip(names, p[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_gflops(a, b, target_s: float = 12.0, dtype=np.float32):
+    """OpenMP Gustavson on a seeded stride sample of A's rows, sized to about
+    target_s seconds; returns (GFLOP/s, threads, sample description)."""
+    import oracle
+    threads = oracle.max_threads()
+    rng = np.random.Generator(np.random.PCG64(0xC0FFEE))
+
+    def sample(frac):
+        k = max(1, int(round(1.0 / frac)))
+        off = int(rng.integers(0, k))
+        rows = np.arange(off, a.m, k, dtype=np.int64)
+        lens = np.diff(a.row_ptr)[rows]
+        rp = np.zeros(rows.size + 1, np.int64)
+        np.cumsum(lens, out=rp[1:])
+        idx = np.concatenate([np.arange(a.row_ptr[r], a.row_ptr[r + 1]) for r in rows]) if rows.size else \
+            np.zeros(0, np.int64)
+        s = synth.CSR(rows.size, a.n, rp.astype(np.int32), a.col_idx[idx], a.val[idx].astype(dtype))
+        return s, k
+
+    frac = 0.01
+    s, k = sample(frac)
+    p = synth.products(s, b)
+    t0 = time.perf_counter()
+    oracle.gustavson_rows(s, b, 0, s.m, dtype)
+    dt = max(time.perf_counter() - t0, 1e-4)
+    frac = min(1.0, frac * target_s / dt)
+    s, k = sample(frac)
+    p = synth.products(s, b)
+    t0 = time.perf_counter()
+    oracle.gustavson_rows(s, b, 0, s.m, dtype)
+    dt = time.perf_counter() - t0
+    return 2.0 * p / dt / 1e9, threads, f"every {k}-th row of A ({s.m} rows, {p} products), {dt:.1f} s"
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    a, b, cfg = workload(args.workload)
+    import oracle
+    dtype = np.float64 if a.val.dtype == np.float64 else np.float32
+    vals = []
+    desc = ""
+    threads = oracle.max_threads()
+    for i in range(args.warmup + args.steps):
+        g, threads, desc = cpu_gflops(a, b, target_s=args.ref_step_s, dtype=dtype)
+        if i >= args.warmup:
+            vals.append(g)
+    v = statistics.mean(vals)
+    line = {"impl": "reference", "metric": "SpGEMM GFLOP/s", "value": v, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": np.dtype(dtype).name,
+            "data": "synthetic", "config": cfg, "vs_baseline": None,
+            "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                             "sample": "OpenMP row-parallel Gustavson (CPU oracle's restatement of "
+                                       "src/spgemm_raw_v2.cu:289-338), " + desc},
+            "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    from gpu_spgemm_gb300 import api
+    a, b, cfg = workload(args.workload)
+    dtype = a.val.dtype
+    v = 8 if dtype == np.float64 else 4
+    stream = torch.cuda.Stream()
+    h = api.Handle(local, stream)
+    A = api.csr2tile(h, a)
+    B = api.build_csc_tiles(h, b)
+    products = api.products(h, A, B)
+    flops = 2.0 * products
+
+    def step():
+        C = api.spgemm(h, A, B, algo=args.algo, prec=args.prec)
+        st = h.stats()
+        info = (C.numtileC, C.nnzC, C.pairs)
+        C.free()
+        return st, info
+
+    for _ in range(args.warmup):
+        step()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stats = []
+    info = None
+    for _ in range(args.steps):
+        st, info = step()
+        stats.append(st)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms = float(t.item())
+    numtileC, nnzC, pairs = info
+    value = world * flops / (ms * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel (CUDA events around it inside the library)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    s1 = statistics.mean(s["ms_step1"] for s in stats)
+    s2 = statistics.mean(s["ms_step2"] for s in stats)
+    s3 = statistics.mean(s["ms_step3"] for s in stats)
+    a_b = tile_bytes(A.numtile, A.nnz, A.tilem, v)
+    b_b = tile_bytes(B.numtile, B.nnz, B.tilem, v, b_side=True)
+    c_b = c_bytes(numtileC, nnzC, A.tilem, v)
+    # numeric kernel: reads A and B tiles and C's structure, writes C's values and column bytes
+    num_bytes = (a_b + b_b + 4 * (A.tilem + 1) + numtileC * (4 + 4 + 8 + 32 + 16) + nnzC * (v + 1))
+    sym_bytes = (4 * (A.tilem + 1) + A.numtile * (4 + 4 + 16) + A.nnz + B.numtile * (4 + 32) + 4 * (B.tilen + 1)
+                 + numtileC * (4 + 4 + 32 + 16 + 4))
+    steps_ms = {"step1": s1, "step2": s2, "step3": s3}
+    dom = max(steps_ms, key=steps_ms.get)
+    dom_bytes = {"step1": 4 * (A.tilem + 1) * 2 + 4 * A.numtile + 4 * B.numtile + 8 * numtileC,
+                 "step2": sym_bytes, "step3": num_bytes}[dom]
+    achieved = dom_bytes / (steps_ms[dom] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": {"step1": "c1_count/fill", "step2": "c2_symbolic",
+                                           "step3": "c3_numeric"}[dom] if args.algo != "rowwise" else dom,
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "peak_source": peak_src, "algorithmic_bytes": dom_bytes, "ms": steps_ms[dom],
+                "traffic": args.traffic}
+    total_bytes = a_b + b_b + c_b
+    hbm_steps = total_bytes / (ms * 1e-3) / 1e9
+
+    # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(h, api, a, b, args, flops, stream)
+
+    # ---- CPU baseline (rank 0 only)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        g, thr, desc = cpu_gflops(a, b, target_s=args.cpu_s, dtype=np.float64 if v == 8 else np.float32)
+        cpu = {"value": g, "unit": "GFLOP/s", "cores": thr, "kind": "port",
+               "sample": "OpenMP row-parallel Gustavson (CPU oracle's restatement of "
+                         "src/spgemm_raw_v2.cu:289-338), " + desc}
+
+    if rank == 0:
+        cfg = dict(cfg)
+        cfg.update({"products": products, "numtileC": numtileC, "nnzC": nnzC, "tile_pairs": pairs,
+                    "algo": args.algo, "prec": args.prec,
+                    "l2": "inputs and outputs exceed L2 (A,B tiles %.2f GB, C %.1f GB > 129 MB)" %
+                          ((a_b + b_b) / 1e9, c_b / 1e9),
+                    "ms_step1": s1, "ms_step2": s2, "ms_step3": s3,
+                    "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak})
+        line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": np.dtype(dtype).name, "data": "synthetic",
+                "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": gpu_launches(args.algo) * args.steps}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def gpu_launches(algo):
+    # plain path per step: step1 count + scan + i64->i32 + fill, step2 symbolic + scan, step3 numeric
+    return 7
+
+
+def measure_e2e(h, api, a, b, args, flops, stream):
+    """End to end through the C ABI with host buffers, per step: the CSR inputs
+    are copied from pinned host memory to the device and tiled, C = A*B is
+    computed, and every array of C is copied back to pinned host memory.  C can
+    exceed host memory (R-MAT 2^20: ~160 GB), so it streams through a fixed
+    pinned staging area in tile ranges (spg_ctiles_to_host_range)."""
+    import torch
+    import ctypes as C
+    from gpu_spgemm_gb300 import _lib as L
+
+    def pin(x):
+        t = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+        return t, t.numpy()
+
+    ha = [pin(a.row_ptr), pin(a.col_idx), pin(a.val)]
+    hb = [pin(b.row_ptr), pin(b.col_idx), pin(b.val)]
+    code = L.SPG_F64 if a.val.dtype == np.float64 else L.SPG_F32
+    vd = np.float64 if code == L.SPG_F64 else np.float32
+    h2d = sum(x[1].nbytes for x in ha + hb)
+    CT = 1 << 24            # C tiles per staged range
+    VC = 1 << 28            # values per staged range
+    st = dict(r=pin(np.zeros(CT, np.int32)), c=pin(np.zeros(CT, np.int32)), m=pin(np.zeros(CT * TS, np.uint16)),
+              p=pin(np.zeros(CT + 1, np.int64)), pr=pin(np.zeros(CT * TS, np.uint8)),
+              v=pin(np.zeros(VC, vd)), cc=pin(np.zeros(VC, np.uint8)), tp=None)
+    lib = h.lib
+
+    def one():
+        ta, tb, c = L.SpgTiles(), L.SpgTiles(), L.SpgCTiles()
+        h.check(lib.spg_tile_from_csr_host(h.h, a.m, a.n, a.nnz, ha[0][1].ctypes.data, ha[1][1].ctypes.data,
+                                           ha[2][1].ctypes.data, code, L.SPG_LAYOUT_ROW, 0, C.byref(ta)))
+        h.check(lib.spg_tile_from_csr_host(h.h, b.m, b.n, b.nnz, hb[0][1].ctypes.data, hb[1][1].ctypes.data,
+                                           hb[2][1].ctypes.data, code, L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
+        h.check(lib.spg_spgemm(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], api._PRECS[args.prec],
+                               C.byref(c)))
+        tp = np.zeros(c.tilem + 1, np.int32)
+        h.check(lib.spg_ctiles_to_host(h.h, C.byref(c), tp.ctypes.data, None, None, None, None, None, None, None))
+        d2h = tp.nbytes
+        nt = c.numtileC
+        t0 = 0
+        step = CT
+        nv = C.c_int64()
+        while t0 < nt:
+            t1 = min(nt, t0 + step)
+            s_ = lib.spg_ctiles_to_host_range(h.h, C.byref(c), t0, t1, st["r"][1].ctypes.data,
+                                              st["c"][1].ctypes.data, st["m"][1].ctypes.data,
+                                              st["p"][1].ctypes.data, st["pr"][1].ctypes.data,
+                                              st["v"][1].ctypes.data, st["cc"][1].ctypes.data, VC, C.byref(nv))
+            if s_ == L.SPG_ERR_INVALID and step > 1:
+                step //= 2
+                continue
+            h.check(s_)
+            d2h += (t1 - t0) * (4 + 4 + 32 + 8 + 16) + 8 + nv.value * (np.dtype(vd).itemsize + 1)
+            t0 = t1
+            step = CT
+        lib.spg_ctiles_free(h.h, C.byref(c))
+        lib.spg_tiles_free(h.h, C.byref(ta))
+        lib.spg_tiles_free(h.h, C.byref(tb))
+        return d2h
+
+    try:
+        one()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        steps = max(1, args.e2e_steps)
+        d2h = 0
+        for _ in range(steps):
+            d2h = one()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": dt * 1e3, "steps": steps,
+                "path": "spg_tile_from_csr_host x2 + spg_spgemm + spg_ctiles_to_host(_range) into pinned host "
+                        "staging (%d tiles / %d values per range)" % (CT, VC)}
+    except Exception as e:  # report instead of dying
+        return {"value": None, "unit": "GFLOP/s", "error": str(e)[:200], "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": None}
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="rmat20")
+    p.add_argument("--algo", default="auto", choices=["auto", "plain", "rowwise"])
+    p.add_argument("--prec", default="f32", choices=["f32", "mixed", "f64"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-s", type=float, default=12.0)
+    p.add_argument("--ref-step-s", type=float, default=8.0)
+    p.add_argument("--traffic", type=float, default=None,
+                   help="dram bytes per launch of the dominant kernel from an ncu capture")
+    args = p.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

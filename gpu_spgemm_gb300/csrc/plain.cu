@@ -1,0 +1,419 @@
+// plain.cu -- the plain tiled SpGEMM kernels: the reference's three steps
+// (src/spgemm_raw_kernels.cuh:23-215, src/spgemm_raw_kernels_v2.cuh:10-139)
+// written from scratch for sm_103a.  One thread block per C tile-row for the
+// structure, one half-warp per C tile for the symbolic phase, one warp per C
+// tile with register accumulators for the numeric phase.  This is the baseline
+// the row-wise binned path is measured against.
+#include "spg_common.cuh"
+#include "plain.cuh"
+
+namespace {
+
+constexpr int C1_THREADS = 256;
+constexpr int C1_WARPS = C1_THREADS / 32;
+constexpr int SPEC_MAX = 32;  // pairs cached per C tile (MAX_MATCHED)
+
+// Union of B's tile columns over A's tiles (i,k) as a bitmap over tilenB.
+// Returns the number of tile pairs visited (valid in every thread's lane 0
+// partial; summed by the caller).
+__device__ int64_t build_c_bitmap(int i, int nwords, const int* __restrict__ a_tp,
+                                  const int* __restrict__ a_tc, const int* __restrict__ b_tp,
+                                  const int* __restrict__ b_tc, uint32_t* bm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int w = threadIdx.x; w < nwords; w += C1_THREADS) bm[w] = 0u;
+    __syncthreads();
+    int64_t pairs = 0;
+    const int as = a_tp[i], ae = a_tp[i + 1];
+    for (int a = as + warp; a < ae; a += C1_WARPS) {
+        const int k = __ldg(&a_tc[a]);
+        const int bs = __ldg(&b_tp[k]), be = __ldg(&b_tp[k + 1]);
+        pairs += be - bs;
+        for (int b = bs + lane; b < be; b += 32) {
+            const int j = __ldg(&b_tc[b]);
+            const uint32_t bit = 1u << (j & 31);
+            if (!(bm[j >> 5] & bit)) atomicOr(&bm[j >> 5], bit);
+        }
+    }
+    __syncthreads();
+    return lane == 0 ? pairs : 0;
+}
+
+__global__ void __launch_bounds__(C1_THREADS)
+c1_count_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
+                const int* __restrict__ b_tp, const int* __restrict__ b_tc, int* __restrict__ cnt,
+                int64_t* __restrict__ row_pairs, unsigned long long* __restrict__ pairs_total) {
+    extern __shared__ uint32_t bm[];
+    __shared__ int s_c[C1_WARPS];
+    __shared__ int64_t s_p[C1_WARPS];
+    const int i = blockIdx.x;
+    if (a_tp[i] == a_tp[i + 1]) {
+        if (threadIdx.x == 0) { cnt[i] = 0; row_pairs[i] = 0; }
+        return;
+    }
+    int64_t pairs = build_c_bitmap(i, nwords, a_tp, a_tc, b_tp, b_tc, bm);
+    int c = 0;
+    for (int w = threadIdx.x; w < nwords; w += C1_THREADS) c += __popc(bm[w]);
+    c = warp_sum(c);
+    pairs = warp_sum(pairs);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_c[warp] = c; s_p[warp] = pairs; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        int64_t p = 0;
+        for (int w = 0; w < C1_WARPS; w++) { t += s_c[w]; p += s_p[w]; }
+        cnt[i] = t;
+        row_pairs[i] = p;
+        if (p) atomicAdd(pairs_total, (unsigned long long)p);
+    }
+}
+
+__global__ void __launch_bounds__(C1_THREADS)
+c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
+               const int* __restrict__ b_tp, const int* __restrict__ b_tc,
+               const int* __restrict__ tile_ptrC, int* __restrict__ rowidxC, int* __restrict__ colidxC) {
+    extern __shared__ uint32_t bm[];
+    __shared__ int64_t s_sh[C1_WARPS + 1];
+    const int i = blockIdx.x;
+    if (tile_ptrC[i] == tile_ptrC[i + 1]) return;
+    build_c_bitmap(i, nwords, a_tp, a_tc, b_tp, b_tc, bm);
+    const int wpt = (nwords + C1_THREADS - 1) / C1_THREADS;
+    const int w0 = min(nwords, (int)threadIdx.x * wpt), w1 = min(nwords, w0 + wpt);
+    int64_t local = 0;
+    for (int w = w0; w < w1; w++) local += __popc(bm[w]);
+    int64_t tot;
+    int64_t run = block_excl_scan<int64_t>(local, s_sh, &tot);
+    int64_t pos = (int64_t)tile_ptrC[i] + run;
+    for (int w = w0; w < w1; w++) {
+        uint32_t bits = bm[w];
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            rowidxC[pos] = i;
+            colidxC[pos] = w * 32 + b;
+            pos++;
+            bits &= bits - 1u;
+        }
+    }
+}
+
+__device__ __forceinline__ int lower_bound_dev(const int* __restrict__ a, int lo, int hi, int key) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a[mid]) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Step 2, one half-warp per C tile.  Matched pairs come from binary-searching
+// the shorter tile list in the longer one (src/spgemm_raw_kernels.cuh:146-158);
+// each pair ORs B's row masks selected by A's column bytes into C's 16 row
+// masks (:173-184); up to SPEC_MAX pairs are cached for step 3 with the bound
+// checked before any write (the reference writes past its buffer first).
+template <bool CACHE>
+__global__ void __launch_bounds__(128)
+c2_symbolic_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
+                   const int* __restrict__ a_tp, const int* __restrict__ a_tc,
+                   const int* __restrict__ a_tnnz, const uint8_t* __restrict__ a_col,
+                   const uint8_t* __restrict__ a_ptr16, const int* __restrict__ b_cscp,
+                   const int* __restrict__ b_cscr, const uint16_t* __restrict__ b_mask,
+                   uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC, int* __restrict__ tile_cnt,
+                   int* __restrict__ spec_cnt, int* __restrict__ spec_off, int* __restrict__ spec_pa,
+                   int* __restrict__ spec_pb, int64_t spec_cap, unsigned long long* __restrict__ alloc_ctr,
+                   unsigned long long* __restrict__ pairs_total, unsigned* flags) {
+    __shared__ int s_pa[8][SPEC_MAX];
+    __shared__ int s_pb[8][SPEC_MAX];
+    const int lane = threadIdx.x & 31, r = lane & 15, half = lane >> 4;
+    const int hw = threadIdx.x >> 4;  // half-warp in block
+    const unsigned hmask = 0xffffu << (16 * half);
+    unsigned long long my_pairs = 0;
+    const int64_t nhw = (int64_t)gridDim.x * 8;
+    for (int64_t t = (int64_t)blockIdx.x * 8 + hw; t < numtileC; t += nhw) {
+        const int bi = rowidxC[t], bj = colidxC[t];
+        const int as = a_tp[bi], ae = a_tp[bi + 1];
+        const int bs = b_cscp[bj], be = b_cscp[bj + 1];
+        const bool a_short = (ae - as) <= (be - bs);
+        const int ss = a_short ? as : bs, se = a_short ? ae : be;
+        const int ls = a_short ? bs : as, le = a_short ? be : ae;
+        const int* sl = a_short ? a_tc : b_cscr;
+        const int* ll = a_short ? b_cscr : a_tc;
+        uint32_t rm = 0;
+        int nm = 0;
+        for (int base = ss; base < se; base += 16) {
+            const int idx = base + r;
+            int pos = -1;
+            if (idx < se) {
+                const int key = __ldg(&sl[idx]);
+                const int p = lower_bound_dev(ll, ls, le, key);
+                if (p < le && __ldg(&ll[p]) == key) pos = p;
+            }
+            unsigned mm = (__ballot_sync(hmask, pos >= 0) >> (16 * half)) & 0xffffu;
+            while (mm) {
+                const int src = __ffs(mm) - 1;
+                mm &= mm - 1u;
+                const int sp = __shfl_sync(hmask, idx, src, 16);
+                const int lp = __shfl_sync(hmask, pos, src, 16);
+                const int pa = a_short ? sp : lp, pb = a_short ? lp : sp;
+                if (CACHE && r == 0 && nm < SPEC_MAX) { s_pa[hw][nm] = pa; s_pb[hw][nm] = pb; }
+                nm++;
+                const int s = __ldg(&a_tnnz[pa]), na = __ldg(&a_tnnz[pa + 1]) - s;
+                const int rs = __ldg(&a_ptr16[(int64_t)pa * TS + r]);
+                const int re = (r == TS - 1) ? na : (int)__ldg(&a_ptr16[(int64_t)pa * TS + r + 1]);
+                for (int e = rs; e < re; e++)
+                    rm |= __ldg(&b_mask[(int64_t)pb * TS + (__ldg(&a_col[s + e]) & 15)]);
+            }
+        }
+        my_pairs += (r == 0) ? (unsigned long long)nm : 0ull;
+        if (CACHE) {
+            __syncwarp(hmask);
+            int off = -1, cached = -1;
+            if (r == 0) {
+                if (nm >= 1 && nm <= SPEC_MAX) {
+                    unsigned long long o = atomicAdd(alloc_ctr, (unsigned long long)nm);
+                    if ((int64_t)(o + nm) <= spec_cap) { off = (int)o; cached = nm; }
+                    else atomicOr(flags, DERR_OVERFLOW);
+                } else if (nm == 0) {
+                    cached = 0;
+                }
+            }
+            off = __shfl_sync(hmask, off, 0, 16);
+            cached = __shfl_sync(hmask, cached, 0, 16);
+            if (cached > 0)
+                for (int q = r; q < cached; q += 16) { spec_pa[off + q] = s_pa[hw][q]; spec_pb[off + q] = s_pb[hw][q]; }
+            if (r == 0) { spec_cnt[t] = cached; spec_off[t] = off; }
+            __syncwarp(hmask);
+        }
+        maskC[t * TS + r] = (uint16_t)rm;
+        int pc = __popc(rm);
+        int inc = pc;
+#pragma unroll
+        for (int d = 1; d < 16; d <<= 1) {
+            const int o = __shfl_up_sync(hmask, inc, d, 16);
+            if (r >= d) inc += o;
+        }
+        ptrRowC[t * TS + r] = (uint8_t)(inc - pc);
+        if (r == TS - 1) tile_cnt[t] = inc;
+    }
+    my_pairs = warp_sum(my_pairs);
+    if (lane == 0 && my_pairs) atomicAdd(pairs_total, my_pairs);
+}
+
+// Step 3, one warp per C tile: lane = (row r, half h); the two halves take
+// alternate A entries of row r (src/spgemm_raw_kernels_v2.cuh:36-37,83) and
+// keep 16 register accumulators; B's row is walked through its 16-bit mask
+// with predicated FMAs instead of the reference's 16-way switch; a shuffle
+// combines the halves and half 0 compacts the row by maskC.
+template <typename V, bool CACHE>
+__global__ void __launch_bounds__(256)
+c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
+                  const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ a_tnnz,
+                  const V* __restrict__ a_val, const uint8_t* __restrict__ a_col,
+                  const uint8_t* __restrict__ a_ptr16, const int* __restrict__ b_cscp,
+                  const int* __restrict__ b_cscr, const int* __restrict__ b_tnnz,
+                  const V* __restrict__ b_val, const uint8_t* __restrict__ b_ptr16,
+                  const uint16_t* __restrict__ b_mask, const int64_t* __restrict__ tile_nnzC,
+                  const uint16_t* __restrict__ maskC, const uint8_t* __restrict__ ptrRowC,
+                  V* __restrict__ valC, uint8_t* __restrict__ colC, const int* __restrict__ spec_cnt,
+                  const int* __restrict__ spec_off, const int* __restrict__ spec_pa,
+                  const int* __restrict__ spec_pb) {
+    const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < numtileC; t += nwarps) {
+        const int64_t cbase = tile_nnzC[t];
+        if (tile_nnzC[t + 1] == cbase) continue;
+        V acc[TS];
+#pragma unroll
+        for (int c = 0; c < TS; c++) acc[c] = V(0);
+        auto do_pair = [&](int pa, int pb) {
+            const int sA = __ldg(&a_tnnz[pa]), na = __ldg(&a_tnnz[pa + 1]) - sA;
+            const int rs = __ldg(&a_ptr16[(int64_t)pa * TS + r]);
+            const int re = (r == TS - 1) ? na : (int)__ldg(&a_ptr16[(int64_t)pa * TS + r + 1]);
+            const int sB = __ldg(&b_tnnz[pb]);
+            for (int e = rs + hsel; e < re; e += 2) {
+                const int kk = __ldg(&a_col[sA + e]) & 15;
+                const V va = __ldg(&a_val[sA + e]);
+                const uint32_t mb = __ldg(&b_mask[(int64_t)pb * TS + kk]);
+                int off = sB + __ldg(&b_ptr16[(int64_t)pb * TS + kk]);
+#pragma unroll
+                for (int c = 0; c < TS; c++) {
+                    if (mb & (0x8000u >> c)) {
+                        acc[c] = fma(va, __ldg(&b_val[off]), acc[c]);
+                        off++;
+                    }
+                }
+            }
+        };
+        int cnt = CACHE ? spec_cnt[t] : -1;
+        if (cnt >= 0) {
+            const int off = spec_off[t];
+            for (int q = 0; q < cnt; q++) do_pair(spec_pa[off + q], spec_pb[off + q]);
+        } else {
+            const int bi = rowidxC[t], bj = colidxC[t];
+            const int as = a_tp[bi], ae = a_tp[bi + 1];
+            const int bs = b_cscp[bj], be = b_cscp[bj + 1];
+            const bool a_short = (ae - as) <= (be - bs);
+            const int ss = a_short ? as : bs, se = a_short ? ae : be;
+            const int ls = a_short ? bs : as, le = a_short ? be : ae;
+            const int* sl = a_short ? a_tc : b_cscr;
+            const int* ll = a_short ? b_cscr : a_tc;
+            for (int base = ss; base < se; base += 32) {
+                const int idx = base + lane;
+                int pos = -1;
+                if (idx < se) {
+                    const int key = __ldg(&sl[idx]);
+                    const int p = lower_bound_dev(ll, ls, le, key);
+                    if (p < le && __ldg(&ll[p]) == key) pos = p;
+                }
+                unsigned mm = __ballot_sync(0xffffffffu, pos >= 0);
+                while (mm) {
+                    const int src = __ffs(mm) - 1;
+                    mm &= mm - 1u;
+                    const int sp = __shfl_sync(0xffffffffu, idx, src);
+                    const int lp = __shfl_sync(0xffffffffu, pos, src);
+                    do_pair(a_short ? sp : lp, a_short ? lp : sp);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < TS; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+        if (hsel == 0) {
+            const uint32_t mc = maskC[t * TS + r];
+            int64_t p = cbase + ptrRowC[t * TS + r];
+#pragma unroll
+            for (int c = 0; c < TS; c++) {
+                if (mc & (0x8000u >> c)) {
+                    valC[p] = acc[c];
+                    colC[p] = (uint8_t)((r << 4) | c);
+                    p++;
+                }
+            }
+        }
+    }
+}
+
+__global__ void i64_to_i32_kernel(const int64_t* __restrict__ in, int* __restrict__ out, int64_t n) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        out[t] = (int)in[t];
+}
+
+int grid_cap(spg_handle_t h, int64_t units, int per_block, int per_sm) {
+    int64_t g = ceil_div(units, per_block);
+    const int64_t cap = (int64_t)h->num_sms * per_sm;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                       int64_t* row_pairs, unsigned long long* pairs_total) {
+    const int tilem = A->tilem;
+    const int nwords = (B->tilen + 31) / 32;
+    const size_t smem = sizeof(uint32_t) * (size_t)nwords;
+    if (smem > h->smem_optin)
+        return spg_fail(h, SPG_ERR_UNSUPPORTED, "step 1: B has too many tile columns for one bitmap");
+    SPG_CUDA(h, cudaFuncSetAttribute(c1_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SPG_CUDA(h, cudaFuncSetAttribute(c1_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int* cnt = nullptr;
+    int64_t* ptr64 = nullptr;
+    SPG_TRY(spg_alloc_t(h, &cnt, (size_t)tilem + 1));
+    SPG_TRY(spg_alloc_t(h, &ptr64, (size_t)tilem + 1));
+    if (tilem > 0) {
+        c1_count_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx,
+                                                               B->tile_ptr, B->tile_columnidx, cnt, row_pairs,
+                                                               pairs_total);
+        SPG_CUDA(h, cudaGetLastError());
+    }
+    SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
+    int64_t numtileC = 0;
+    SPG_TRY(spg_read_i64(h, ptr64 + tilem, &numtileC));
+    if (numtileC > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "C has more than 2^31-1 tiles");
+    C->numtileC = numtileC;
+    SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
+    i64_to_i32_kernel<<<grid_cap(h, tilem + 1, 256, 8), 256, 0, h->stream>>>(ptr64, C->tile_ptrC, tilem + 1);
+    SPG_CUDA(h, cudaGetLastError());
+    SPG_TRY(spg_alloc_t(h, &C->tile_rowidxC, (size_t)numtileC + 1));
+    SPG_TRY(spg_alloc_t(h, &C->tile_colidxC, (size_t)numtileC + 1));
+    if (tilem > 0 && numtileC > 0) {
+        c1_fill_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
+                                                              B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
+                                                              C->tile_colidxC);
+        SPG_CUDA(h, cudaGetLastError());
+    }
+    spg_free_async(h, cnt);
+    spg_free_async(h, ptr64);
+    return SPG_OK;
+}
+
+spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                       PlainPriv* pp, int* tile_cnt) {
+    const int64_t nt = C->numtileC;
+    unsigned long long* ctr = pp->counters;  // [0] alloc, [1] pairs
+    SPG_CUDA(h, cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), h->stream));
+    if (nt == 0) return SPG_OK;
+    const int grid = grid_cap(h, nt, 8, 64);
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (pp->spec_cap > 0) {
+            c2_symbolic_kernel<true><<<grid, 128, 0, h->stream>>>(
+                nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, A->tile_csr_Col,
+                A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, tile_cnt,
+                pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb, pp->spec_cap, ctr, ctr + 1, h->d_flags);
+        } else {
+            c2_symbolic_kernel<false><<<grid, 128, 0, h->stream>>>(
+                nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, A->tile_csr_Col,
+                A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, tile_cnt,
+                nullptr, nullptr, nullptr, nullptr, 0, ctr, ctr + 1, h->d_flags);
+        }
+        SPG_CUDA(h, cudaGetLastError());
+        if (pp->spec_cap == 0) break;
+        // overflow re-run (src/spgemm_raw_v2.cu:191-200, with the bound honoured in-kernel)
+        int64_t used = 0;
+        SPG_TRY(spg_read_i64(h, (const int64_t*)ctr, &used));
+        unsigned fl = 0;
+        SPG_CUDA(h, cudaMemcpy(&fl, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (!(fl & DERR_OVERFLOW)) break;
+        SPG_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
+        h->stats.overflow_reruns++;
+        spg_free_async(h, pp->spec_pa);
+        spg_free_async(h, pp->spec_pb);
+        pp->spec_pa = pp->spec_pb = nullptr;
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        if (attempt == 0 && (size_t)used * 8 < fr / 2) {
+            pp->spec_cap = used;
+            SPG_TRY(spg_alloc_t(h, &pp->spec_pa, (size_t)used + 1));
+            SPG_TRY(spg_alloc_t(h, &pp->spec_pb, (size_t)used + 1));
+            SPG_CUDA(h, cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), h->stream));
+        } else {
+            pp->spec_cap = 0;  // numeric recomputes the intersections
+            SPG_CUDA(h, cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), h->stream));
+        }
+    }
+    return SPG_OK;
+}
+
+template <typename V>
+static spg_status plain_step3_t(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                                PlainPriv* pp) {
+    const int64_t nt = C->numtileC;
+    if (nt == 0 || C->nnzC == 0) return SPG_OK;
+    const int grid = grid_cap(h, nt, 8, 32);
+    if (pp && pp->spec_cap > 0)
+        c3_numeric_kernel<V, true><<<grid, 256, 0, h->stream>>>(
+            nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
+            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,
+            (V*)C->tile_valC, C->tile_colC, pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb);
+    else
+        c3_numeric_kernel<V, false><<<grid, 256, 0, h->stream>>>(
+            nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
+            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,
+            (V*)C->tile_valC, C->tile_colC, nullptr, nullptr, nullptr, nullptr);
+    SPG_CUDA(h, cudaGetLastError());
+    return SPG_OK;
+}
+
+spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp) {
+    if (A->dtype == SPG_F64) return plain_step3_t<double>(h, A, B, C, pp);
+    return plain_step3_t<float>(h, A, B, C, pp);
+}

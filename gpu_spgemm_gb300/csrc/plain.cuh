@@ -1,0 +1,24 @@
+// plain.cuh -- interface of the plain per-C-tile kernels (plain.cu).
+#pragma once
+#include "spg_common.cuh"
+
+// Per-C private state of the plain path: the matched-pair cache of step 2
+// (spec_* in src/spgemm_raw_v2.cu:161-172) and two device counters.
+struct PlainPriv {
+    int* spec_cnt = nullptr;   // numtileC: cached pair count, -1 = not cached
+    int* spec_off = nullptr;   // numtileC
+    int* spec_pa = nullptr;    // spec_cap
+    int* spec_pb = nullptr;    // spec_cap
+    int64_t spec_cap = 0;
+    unsigned long long* counters = nullptr;  // [0] cache allocation, [1] matched pairs (step 2), [2] tile pairs (step 1)
+};
+
+spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                       int64_t* row_pairs, unsigned long long* pairs_total);
+spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                       PlainPriv* pp, int* tile_cnt);
+spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                       PlainPriv* pp);
+
+spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int* d_rp, const int* d_ci,
+                           const void* d_val, spg_dtype dtype, spg_layout layout, int flags, spg_tiles* out);

@@ -1,0 +1,459 @@
+// rowwise.cu -- row-wise (Gustavson-order) tiled SpGEMM: the bitmask symbolic
+// phase and the numeric phase organised per C tile-row instead of per C tile.
+//
+// Same outputs as the per-C-tile kernels (plain.cu), bit for bit in the
+// structure: row r of C tile (i,j) is the OR over A's nonzeros (r,k) of the
+// 16-bit row mask of B's tile (k/16, j) at row k%16 -- exactly the reference's
+// OR of maskB rows over matched tile pairs (src/spgemm_raw_kernels.cuh:173-184)
+// -- but the pairs are enumerated from A's rows and B's rows instead of by
+// intersecting A's tile-row list with B's tile-column list for every C tile.
+// On a power-law matrix (R-MAT, 2^20) the intersections cost 1.1e11 probes
+// against 2.1e10 products; this order touches every product once.
+//
+// Work decomposition (GB300: 152 SMs, 227 KB shared memory per CTA):
+//   work item  = (C tile-row i, region of <= RT consecutive C tiles)
+//   persistent CTAs take items from an atomic ticket (biggest tile-rows first,
+//   in natural order);
+//   a region is walked in shared-memory windows (symbolic: WS tiles of 16 row
+//   masks; numeric: <= NW_MAXT tiles and <= NW_VALS values of C);
+//   per A nonzero of the tile-row a cursor into its B row carries over from
+//   window to window, so B's rows are read once per region, never searched
+//   per window;
+//   a B entry (c, v) finds its C tile by a popcount rank in a bitmap of the
+//   window's tile columns, its value slot by popc of the C row mask.
+#include <climits>
+
+#include "rowwise.cuh"
+
+namespace {
+
+constexpr int RW_THREADS = 512;
+constexpr int RW_WARPS = RW_THREADS / 32;
+constexpr int RT = 16384;       // C tiles per work item
+constexpr int WS = 2048;        // C tiles per symbolic window
+constexpr int NW_MAXT = 1024;   // C tiles per numeric window
+constexpr int NW_VALS = 8192;   // C values per numeric window
+constexpr int MAXA_SMEM = 2048; // A nonzeros per tile-row whose cursors fit in shared memory
+
+__device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a[mid]) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void rw_plan_kernel(int tilem, int m, const int* __restrict__ tile_ptrC, const int* __restrict__ a_rp,
+                               int64_t* __restrict__ nitems, unsigned long long* __restrict__ max_na) {
+    unsigned long long mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
+        const int ntc = tile_ptrC[i + 1] - tile_ptrC[i];
+        nitems[i] = ntc > 0 ? (ntc + RT - 1) / RT : 0;
+        const int na = a_rp[min(i * TS + TS, m)] - a_rp[i * TS];
+        if (ntc > 0 && (unsigned long long)na > mx) mx = (unsigned long long)na;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, d);
+        mx = o > mx ? o : mx;
+    }
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_na, mx);
+}
+
+// Shared state of one work item.
+struct ItemInfo {
+    int i, rs, re, e0, na, q;
+};
+
+// Takes the next work item; returns false when none is left.  All threads call.
+__device__ bool next_item(unsigned long long* ticket, const int64_t* __restrict__ item_prefix, int tilem,
+                          int64_t nitems, const int* __restrict__ tile_ptrC, const int* __restrict__ a_rp, int m,
+                          ItemInfo* s_it, int* s_rows) {
+    __shared__ long long s_item;
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(ticket, 1ull);
+    __syncthreads();
+    const int64_t item = s_item;
+    if (item >= nitems) return false;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = tilem;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (item_prefix[mid] <= item) lo = mid; else hi = mid;
+        }
+        const int q = (int)(item - item_prefix[lo]);
+        const int ts = tile_ptrC[lo], te = tile_ptrC[lo + 1];
+        s_it->i = lo;
+        s_it->q = q;
+        s_it->rs = ts + q * RT;
+        s_it->re = min(ts + (q + 1) * RT, te);
+    }
+    __syncthreads();
+    if (threadIdx.x <= TS) {
+        const int r0 = s_it->i * TS;
+        s_rows[threadIdx.x] = a_rp[min(r0 + (int)threadIdx.x, m)];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_it->e0 = s_rows[0];
+        s_it->na = s_rows[TS] - s_rows[0];
+    }
+    __syncthreads();
+    return true;
+}
+
+// Cursor of every A nonzero of the tile-row: first B-row position whose column
+// is >= the region's first column, and that column (INT_MAX past the row end).
+__device__ void init_cursors(const ItemInfo& it, int2* cur, const int* __restrict__ colidxC,
+                             const int* __restrict__ a_ci, const int* __restrict__ b_rp,
+                             const int* __restrict__ b_ci) {
+    const int cstart = colidxC[it.rs] * TS;
+    for (int x = threadIdx.x; x < it.na; x += RW_THREADS) {
+        const int k = __ldg(&a_ci[it.e0 + x]);
+        int b = __ldg(&b_rp[k]);
+        const int be = __ldg(&b_rp[k + 1]);
+        if (it.q > 0) b = lower_bound_i(b_ci, b, be, cstart);
+        cur[x] = make_int2(b, b < be ? __ldg(&b_ci[b]) : INT_MAX);
+    }
+    __syncthreads();
+}
+
+// Bitmap of a window's (sorted, distinct) tile columns plus per-word popcount
+// prefix: rank(j) = index of column j among the window's tiles.
+__device__ void build_window_rank(const int* __restrict__ colidxC, int t0, int nt, int wlo, int nwd,
+                                  uint32_t* bm, uint32_t* pre, int64_t* s_sh) {
+    for (int x = threadIdx.x; x < nwd; x += RW_THREADS) bm[x] = 0u;
+    __syncthreads();
+    for (int x = threadIdx.x; x < nt; x += RW_THREADS) {
+        const int j = colidxC[t0 + x];
+        atomicOr(&bm[(j >> 5) - wlo], 1u << (j & 31));
+    }
+    __syncthreads();
+    const int wpt = (nwd + RW_THREADS - 1) / RW_THREADS;
+    const int a = min(nwd, (int)threadIdx.x * wpt), b = min(nwd, a + wpt);
+    int64_t local = 0;
+    for (int x = a; x < b; x++) local += __popc(bm[x]);
+    int64_t tot;
+    int64_t run = block_excl_scan<int64_t>(local, s_sh, &tot);
+    for (int x = a; x < b; x++) {
+        pre[x] = (uint32_t)run;
+        run += __popc(bm[x]);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ int wrank(const uint32_t* bm, const uint32_t* pre, int wlo, int j) {
+    const int w = (j >> 5) - wlo;
+    return (int)pre[w] + __popc(bm[w] & ((1u << (j & 31)) - 1u));
+}
+
+__device__ __forceinline__ int row_of(const int* s_rows, int e) {
+    int r = 0;
+#pragma unroll
+    for (int q = 1; q < TS; q++) r += (s_rows[q] <= e) ? 1 : 0;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// symbolic
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RW_THREADS)
+rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t nitems,
+                   const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
+                   const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
+                   const int* __restrict__ b_ci, uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC,
+                   int* __restrict__ tile_cnt, unsigned long long* ticket, int2* __restrict__ cursor_g, int max_na) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* masks32 = smem;                      // [16][WS] halfwords
+    int2* cur_s = reinterpret_cast<int2*>(masks32 + WS * 8);
+    uint32_t* bm = reinterpret_cast<uint32_t*>(cur_s + MAXA_SMEM);
+    uint32_t* pre = bm + nwords_b;
+    __shared__ ItemInfo s_it;
+    __shared__ int s_rows[TS + 1];
+    __shared__ int64_t s_sh[RW_WARPS + 1];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
+        const ItemInfo it = s_it;
+        int2* cur = (it.na <= MAXA_SMEM) ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        init_cursors(it, cur, colidxC, a_ci, b_rp, b_ci);
+        for (int w0 = it.rs; w0 < it.re; w0 += WS) {
+            const int nt = min(WS, it.re - w0);
+            const int jlo = colidxC[w0], jhi = colidxC[w0 + nt - 1];
+            const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
+            const int limit = (jhi + 1) * TS;
+            for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
+            build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
+            for (int x = warp; x < it.na; x += RW_WARPS) {
+                const int2 cs = cur[x];
+                if (cs.y >= limit) continue;
+                const int e = it.e0 + x;
+                const int k = __ldg(&a_ci[e]);
+                const int be = __ldg(&b_rp[k + 1]);
+                const int r = row_of(s_rows, e);
+                int p = cs.x, nextc = INT_MAX;
+                while (true) {
+                    const int qq = p + lane;
+                    const int c = qq < be ? __ldg(&b_ci[qq]) : INT_MAX;
+                    const bool in = c < limit;
+                    const unsigned bal = __ballot_sync(0xffffffffu, in);
+                    if (in) {
+                        const int lt = wrank(bm, pre, wlo, c >> 4);
+                        const int idx = r * WS + lt;
+                        atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
+                    }
+                    const int cnt = __popc(bal);
+                    if (cnt < 32) {
+                        nextc = __shfl_sync(0xffffffffu, c, cnt);
+                        p += cnt;
+                        break;
+                    }
+                    p += 32;
+                }
+                if (lane == 0) cur[x] = make_int2(p, nextc);
+            }
+            __syncthreads();
+            for (int x = tid; x < nt; x += RW_THREADS) {
+                uint32_t mw[8];
+                uint32_t pw[4] = {0u, 0u, 0u, 0u};
+                int tot = 0;
+#pragma unroll
+                for (int r = 0; r < TS; r++) {
+                    const int idx = r * WS + x;
+                    const uint32_t m16 = (masks32[idx >> 1] >> ((idx & 1) * 16)) & 0xffffu;
+                    if (r & 1) mw[r >> 1] |= m16 << 16; else mw[r >> 1] = m16;
+                    pw[r >> 2] |= (uint32_t)(tot & 0xff) << (8 * (r & 3));
+                    tot += __popc(m16);
+                }
+                const int64_t t = (int64_t)w0 + x;
+                uint4* mo = reinterpret_cast<uint4*>(maskC) + 2 * t;
+                mo[0] = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                mo[1] = make_uint4(mw[4], mw[5], mw[6], mw[7]);
+                reinterpret_cast<uint4*>(ptrRowC)[t] = make_uint4(pw[0], pw[1], pw[2], pw[3]);
+                tile_cnt[t] = tot;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// numeric
+// ---------------------------------------------------------------------------
+template <typename ACC>
+__device__ __forceinline__ void acc_add(ACC* a, ACC v) { atomicAdd(a, v); }
+
+template <typename V, typename ACC>
+__global__ void __launch_bounds__(RW_THREADS)
+rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t nitems,
+                  const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
+                  const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
+                  const uint8_t* __restrict__ ptrRowC, const int* __restrict__ a_rp, const int* __restrict__ a_ci,
+                  const V* __restrict__ a_val, const int* __restrict__ b_rp, const int* __restrict__ b_ci,
+                  const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
+                  unsigned long long* ticket, int2* __restrict__ cursor_g, int max_na) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    ACC* acc = reinterpret_cast<ACC*>(smem);                                   // NW_VALS + 256
+    uint16_t* mk = reinterpret_cast<uint16_t*>(acc + NW_VALS + 256);           // [NW_MAXT][16]
+    uint8_t* pr = reinterpret_cast<uint8_t*>(mk + NW_MAXT * TS);               // [NW_MAXT][16]
+    int* vbase = reinterpret_cast<int*>(pr + NW_MAXT * TS);                    // NW_MAXT
+    int2* cur_s = reinterpret_cast<int2*>(vbase + NW_MAXT);                    // MAXA_SMEM
+    uint32_t* bm = reinterpret_cast<uint32_t*>(cur_s + MAXA_SMEM);
+    uint32_t* pre = bm + nwords_b;
+    __shared__ ItemInfo s_it;
+    __shared__ int s_rows[TS + 1];
+    __shared__ int64_t s_sh[RW_WARPS + 1];
+    __shared__ int s_nt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
+        const ItemInfo it = s_it;
+        int2* cur = (it.na <= MAXA_SMEM) ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        init_cursors(it, cur, colidxC, a_ci, b_rp, b_ci);
+        int t0 = it.rs;
+        while (t0 < it.re) {
+            // window [t0, t1): at most NW_MAXT tiles and NW_VALS values (a tile holds <= 256)
+            const int64_t v0 = tile_nnzC[t0];
+            const int cap_t = min(NW_MAXT, it.re - t0);
+            if (tid == 0) s_nt = 0;
+            __syncthreads();
+            int ok = 0;
+            for (int x = tid; x < cap_t; x += RW_THREADS) ok += (tile_nnzC[t0 + x + 1] - v0 <= NW_VALS) ? 1 : 0;
+            if (ok) atomicAdd(&s_nt, ok);
+            __syncthreads();
+            const int ntw = max(1, s_nt);
+            const int t1 = t0 + ntw;
+            const int64_t v1 = tile_nnzC[t1];
+            const int nv = (int)(v1 - v0);
+            if (nv == 0) {
+                t0 = t1;
+                __syncthreads();
+                continue;
+            }
+            const int jlo = colidxC[t0], jhi = colidxC[t1 - 1];
+            const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
+            const int limit = (jhi + 1) * TS;
+            for (int x = tid; x < ntw; x += RW_THREADS) {
+                const int64_t t = (int64_t)t0 + x;
+                vbase[x] = (int)(tile_nnzC[t] - v0);
+                const uint4* mi = reinterpret_cast<const uint4*>(maskC) + 2 * t;
+                reinterpret_cast<uint4*>(mk)[2 * x] = mi[0];
+                reinterpret_cast<uint4*>(mk)[2 * x + 1] = mi[1];
+                reinterpret_cast<uint4*>(pr)[x] = reinterpret_cast<const uint4*>(ptrRowC)[t];
+            }
+            for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
+            build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
+            for (int x = warp; x < it.na; x += RW_WARPS) {
+                const int2 cs = cur[x];
+                if (cs.y >= limit) continue;
+                const int e = it.e0 + x;
+                const int k = __ldg(&a_ci[e]);
+                const ACC va = (ACC)__ldg(&a_val[e]);
+                const int be = __ldg(&b_rp[k + 1]);
+                const int r = row_of(s_rows, e);
+                int p = cs.x, nextc = INT_MAX;
+                while (true) {
+                    const int qq = p + lane;
+                    const int c = qq < be ? __ldg(&b_ci[qq]) : INT_MAX;
+                    const bool in = c < limit;
+                    const unsigned bal = __ballot_sync(0xffffffffu, in);
+                    if (in) {
+                        const int lt = wrank(bm, pre, wlo, c >> 4);
+                        const uint32_t m16 = mk[lt * TS + r];
+                        const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
+                        acc_add(&acc[pos], va * (ACC)__ldg(&b_val[qq]));
+                    }
+                    const int cnt = __popc(bal);
+                    if (cnt < 32) {
+                        nextc = __shfl_sync(0xffffffffu, c, cnt);
+                        p += cnt;
+                        break;
+                    }
+                    p += 32;
+                }
+                if (lane == 0) cur[x] = make_int2(p, nextc);
+            }
+            __syncthreads();
+            for (int x = tid; x < nv; x += RW_THREADS) valC[v0 + x] = (V)acc[x];
+            for (int x = tid; x < ntw * TS; x += RW_THREADS) {
+                const int lt = x >> 4, r = x & 15;
+                uint32_t m16 = mk[lt * TS + r];
+                int64_t p = v0 + vbase[lt] + pr[lt * TS + r];
+                while (m16) {
+                    const int c = __clz(m16) - 16;
+                    colC[p++] = (uint8_t)((r << 4) | c);
+                    m16 &= ~(0x8000u >> c);
+                }
+            }
+            __syncthreads();
+            t0 = t1;
+        }
+    }
+}
+
+size_t sym_smem(int nwords_b) {
+    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * 8 + 2 * (size_t)nwords_b * 4;
+}
+
+template <typename ACC>
+size_t num_smem(int nwords_b) {
+    return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 2 + (size_t)NW_MAXT * TS +
+           (size_t)NW_MAXT * 4 + (size_t)MAXA_SMEM * 8 + 2 * (size_t)nwords_b * 4;
+}
+
+}  // namespace
+
+spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B) {
+    const int nwords_b = (B->tilen + 31) / 32;
+    if (num_smem<double>(nwords_b) > h->smem_optin) return SPG_ALGO_PLAIN;
+    (void)A;
+    return SPG_ALGO_ROWWISE;
+}
+
+static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, spg_ctiles* C, RowwisePriv* rp) {
+    if (rp->item_prefix) return SPG_OK;
+    const int tilem = C->tilem;
+    int64_t* nit = nullptr;
+    SPG_TRY(spg_alloc_t(h, &nit, (size_t)tilem + 1));
+    SPG_TRY(spg_alloc_t(h, &rp->item_prefix, (size_t)tilem + 1));
+    SPG_TRY(spg_alloc_t(h, &rp->counters, 4));
+    SPG_CUDA(h, cudaMemsetAsync(rp->counters, 0, 4 * sizeof(unsigned long long), h->stream));
+    if (tilem > 0) {
+        int g = (int)ceil_div(tilem, 256);
+        if (g > h->num_sms * 8) g = h->num_sms * 8;
+        rw_plan_kernel<<<g, 256, 0, h->stream>>>(tilem, A->m, C->tile_ptrC, A->row_ptr, nit, rp->counters + 2);
+        SPG_CUDA(h, cudaGetLastError());
+    }
+    SPG_TRY(spg_scan_i64_to_i64(h, nit, rp->item_prefix, tilem));
+    spg_free_async(h, nit);
+    SPG_TRY(spg_read_i64(h, rp->item_prefix + tilem, &rp->nitems));
+    int64_t mx = 0;
+    SPG_TRY(spg_read_i64(h, (const int64_t*)(rp->counters + 2), &mx));
+    rp->max_na = (int)mx;
+    // persistent grid: as many CTAs as fit (numeric is the larger footprint)
+    int occ = 0;
+    const int nwords_b = (C->tilen + 31) / 32;
+    const size_t smem = num_smem<double>(nwords_b) > sym_smem(nwords_b) ? num_smem<double>(nwords_b)
+                                                                         : sym_smem(nwords_b);
+    SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<double, double>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_numeric_kernel<double, double>, RW_THREADS,
+                                                              smem));
+    if (occ < 1) occ = 1;
+    rp->grid = h->num_sms * occ * 2;
+    if (rp->max_na > MAXA_SMEM) {
+        SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na + 1));
+    }
+    return SPG_OK;
+}
+
+spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
+                            int* tile_cnt) {
+    if (C->numtileC == 0) return SPG_OK;
+    SPG_TRY(rw_prepare(h, A, C, rp));
+    h->stats.work_items = rp->nitems;
+    const int nwords_b = (B->tilen + 31) / 32;
+    const size_t smem = sym_smem(nwords_b);
+    if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise symbolic: B too wide");
+    SPG_CUDA(h, cudaFuncSetAttribute(rw_symbolic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SPG_CUDA(h, cudaMemsetAsync(rp->counters, 0, sizeof(unsigned long long), h->stream));
+    rw_symbolic_kernel<<<rp->grid, RW_THREADS, smem, h->stream>>>(
+        A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, A->row_ptr,
+        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na);
+    SPG_CUDA(h, cudaGetLastError());
+    return SPG_OK;
+}
+
+template <typename V, typename ACC>
+static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                                 RowwisePriv* rp) {
+    const int nwords_b = (B->tilen + 31) / 32;
+    const size_t smem = num_smem<ACC>(nwords_b);
+    if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: B too wide");
+    SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<V, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    SPG_CUDA(h, cudaMemsetAsync(rp->counters + 1, 0, sizeof(unsigned long long), h->stream));
+    rw_numeric_kernel<V, ACC><<<rp->grid, RW_THREADS, smem, h->stream>>>(
+        A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
+        C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
+        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na);
+    SPG_CUDA(h, cudaGetLastError());
+    return SPG_OK;
+}
+
+spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
+                           spg_precision prec) {
+    if (C->numtileC == 0 || C->nnzC == 0) return SPG_OK;
+    SPG_TRY(rw_prepare(h, A, C, rp));
+    if (A->dtype == SPG_F64) return launch_numeric<double, double>(h, A, B, C, rp);
+    if (prec == SPG_PREC_F64) return launch_numeric<float, double>(h, A, B, C, rp);
+    return launch_numeric<float, float>(h, A, B, C, rp);
+}
+
+void rowwise_free_priv(spg_handle_t h, RowwisePriv* rp) {
+    spg_free_async(h, rp->item_prefix);
+    spg_free_async(h, rp->counters);
+    spg_free_async(h, rp->cursor_g);
+    *rp = RowwisePriv{};
+}
+
+void rowwise_free_bview(spg_handle_t, spg_tiles*) {}

@@ -1,0 +1,126 @@
+// spg_common.cuh -- shared definitions for the GB300 tiled SpGEMM kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/spgemm_gb300.h"
+
+#define TS 16
+
+// Device error bits, written to a per-handle flag word by kernels and read
+// back by the host after the call's synchronisation point.
+enum : unsigned {
+    DERR_NONCANONICAL = 1u << 0,  // CSR columns not strictly ascending / out of range
+    DERR_TIMEOUT = 1u << 1,       // a bounded spin-wait gave up
+    DERR_OVERFLOW = 1u << 2,      // a pre-sized buffer was too small (writes skipped)
+    DERR_TOO_BIG = 1u << 3,       // a count overflowed its index type
+};
+
+// Upper bound on spin iterations of any device-side wait (decoupled look-back).
+// Forward progress is guaranteed by ticket ordering; the bound is a safety net
+// that turns a would-be hang into DERR_TIMEOUT.
+#define SPG_SPIN_LIMIT (1 << 22)
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v, unsigned lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= (unsigned)d) v += o;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; `sh` needs blockDim/32 + 1
+// entries.  Returns the exclusive prefix, writes the block total to *total.
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* sh, T* total) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T inc = warp_incl_scan(v, lane);
+    if (lane == 31) sh[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < nw ? sh[lane] : T(0);
+        T wi = warp_incl_scan(w, lane);
+        if (lane < nw) sh[lane] = wi - w;
+        if (lane == nw - 1) sh[nw] = wi;
+    }
+    __syncthreads();
+    T res = sh[warp] + inc - v;
+    *total = sh[nw];
+    __syncthreads();
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct spg_handle_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    spg_stats stats{};
+    unsigned* d_flags = nullptr;      // device error bits
+    int64_t* h_pinned = nullptr;      // 64 pinned words for read-backs
+    cudaEvent_t ev[8]{};
+    int num_sms = 0;
+    size_t smem_optin = 0;
+};
+
+spg_status spg_fail(spg_handle_t h, spg_status s, const std::string& msg);
+spg_status spg_cuda_fail(spg_handle_t h, cudaError_t e, const char* what);
+
+#define SPG_CUDA(h, call)                                              \
+    do {                                                               \
+        cudaError_t _e = (call);                                       \
+        if (_e != cudaSuccess) return spg_cuda_fail((h), _e, #call);   \
+    } while (0)
+
+#define SPG_TRY(call)                          \
+    do {                                       \
+        spg_status _s = (call);                \
+        if (_s != SPG_OK) return _s;           \
+    } while (0)
+
+// Stream-ordered device allocation on the handle's stream.
+spg_status spg_alloc(spg_handle_t h, void** p, size_t bytes);
+void spg_free_async(spg_handle_t h, void* p);
+template <typename T>
+inline spg_status spg_alloc_t(spg_handle_t h, T** p, size_t count) {
+    return spg_alloc(h, reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+// Read device error bits (synchronises the stream) and clear them.
+spg_status spg_check_flags(spg_handle_t h, const char* where);
+
+// Exclusive scans: out[0..n] (n+1 entries, out[n] = total).  `in` may alias
+// `out` when the types match.  Temporary storage comes from spg_alloc.
+spg_status spg_scan_i32_to_i32(spg_handle_t h, const int* in, int* out, int64_t n);
+spg_status spg_scan_i32_to_i64(spg_handle_t h, const int* in, int64_t* out, int64_t n);
+spg_status spg_scan_i64_to_i64(spg_handle_t h, const int64_t* in, int64_t* out, int64_t n);
+
+// Stable LSD radix sort of (key, value) pairs by the low `key_bits` of key.
+spg_status spg_radix_sort_pairs(spg_handle_t h, uint32_t* keys, uint32_t* vals, int64_t n,
+                                int key_bits);
+
+// Read a device scalar (synchronises the stream).
+spg_status spg_read_i64(spg_handle_t h, const int64_t* d, int64_t* out);
+spg_status spg_read_i32(spg_handle_t h, const int* d, int* out);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline size_t val_size(spg_dtype t) { return t == SPG_F64 ? 8 : 4; }

@@ -1,0 +1,223 @@
+/*
+ * spgemm_gb300.h -- C ABI of the GB300 tiled SpGEMM library (libspgemm_gb300.so).
+ *
+ * The library computes C = A * B for sparse matrices stored in the 16x16 tile
+ * format of jianjianh1/GPU_SPGEMM (src/tile_format.h:15-42): per tile-row a tile
+ * pointer, per tile its column, an nnz prefix, 16 per-row uint8 offsets and 16
+ * per-row uint16 occupancy masks (bit 15-c set <=> column c occupied, 256 bits
+ * per tile), per nonzero a value and a column byte.  A is tiled row-major
+ * (column byte = (row<<4)|col); B is tiled in CSC tile order (column byte = col),
+ * exactly as csr2tile / build_csc_tiles lay them out.
+ *
+ * The reference has no library API: its "interface" is the host functions of
+ * tile_format.h, the kernel signatures and the driver sequence of
+ * src/spgemm_raw_v2.cu:101-243.  Each entry point below names the reference code
+ * it replaces.
+ *
+ * Conventions
+ *   - Every call returns an spg_status; spg_last_error() gives a message.
+ *   - Work is ordered on the handle's CUDA stream (given at spg_create).
+ *   - Device buffers inside spg_tiles / spg_ctiles are allocated by the
+ *     library and released by spg_tiles_free / spg_ctiles_free.
+ *   - A handle is not thread safe; use one handle per host thread.
+ *   - Offsets that can exceed 2^31 (C's nnz prefix) are int64; everything the
+ *     reference stores as int stays int32 and the library rejects inputs whose
+ *     counts would overflow it (SPG_ERR_INVALID).
+ */
+#ifndef SPGEMM_GB300_H
+#define SPGEMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPG_TILE 16
+
+typedef enum {
+    SPG_OK = 0,
+    SPG_ERR_INVALID = 1,          /* bad argument or non-canonical CSR           */
+    SPG_ERR_OOM = 2,              /* device allocation failed                    */
+    SPG_ERR_OVERFLOW_RERUN = 3,   /* a pre-sized buffer overflowed; re-run done  */
+    SPG_ERR_TIMEOUT = 4,          /* a bounded device wait gave up               */
+    SPG_ERR_CUDA = 5,             /* CUDA runtime error                          */
+    SPG_ERR_UNSUPPORTED = 6
+} spg_status;
+
+typedef enum { SPG_F32 = 0, SPG_F64 = 1 } spg_dtype;
+
+/* Tiling layouts: ROW = csr2tile (src/tile_format.h:93-222);
+   B_CSC = csr2tile + build_csc_tiles (src/tile_format.h:424-585). */
+typedef enum { SPG_LAYOUT_ROW = 0, SPG_LAYOUT_B_CSC = 1 } spg_layout;
+
+/* spg_tile_from_csr flags */
+#define SPG_TILE_WITH_TILE_CSC 0x1   /* also build tile_csc_Ptr/Row/Val (B only) */
+
+/* Numeric algorithms.  PLAIN: one warp per C tile, matched tile pairs by list
+   intersection, register accumulators (the reference's step 3 structure).
+   ROWWISE: tile-row work items in shared-memory windows, binned by density.
+   AUTO picks per workload. */
+typedef enum { SPG_ALGO_AUTO = 0, SPG_ALGO_PLAIN = 1, SPG_ALGO_ROWWISE = 2 } spg_algo;
+
+/* Precision of the numeric phase for FP32 inputs.  F32: FP32 register path.
+   MIXED: FP32 bulk, tiles above the fill threshold on BF16/FP16 tensor cores
+   with split hi+lo products, FP64 for cancellation-flagged tiles.  FP64
+   inputs always compute in FP64. */
+typedef enum { SPG_PREC_F32 = 0, SPG_PREC_MIXED = 1, SPG_PREC_F64 = 2 } spg_precision;
+
+typedef struct spg_handle_s* spg_handle_t;
+
+/* Device-resident tile matrix: the reference's TileMatrix (src/tile_format.h:15-42)
+   plus the row view used by the row-wise kernels.  All pointers are device
+   pointers owned by the library. */
+typedef struct {
+    int m, n;
+    int64_t nnz;
+    int tilem, tilen;
+    int64_t numtile;
+    spg_dtype dtype;
+    spg_layout layout;
+    /* tile level (row-major tiling, always present) */
+    int* tile_ptr;              /* tilem+1                                     */
+    int* tile_columnidx;        /* numtile                                     */
+    /* per tile, in this layout's tile order (row-major for ROW, CSC for B_CSC) */
+    int* tile_nnz;              /* numtile+1, exclusive prefix                 */
+    uint8_t* tile_csr_Ptr;      /* numtile*16, per-row offset inside the tile  */
+    uint16_t* mask;             /* numtile*16, bit 15-c <=> column c           */
+    void* tile_csr_Val;         /* nnz, float or double                        */
+    uint8_t* tile_csr_Col;      /* nnz, (r<<4)|c for ROW, c for B_CSC          */
+    /* B_CSC only */
+    int* csc_tile_ptr;          /* tilen+1                                     */
+    int* csc_tile_rowidx;       /* numtile                                     */
+    int* csc_to_row;            /* numtile: CSC tile index -> row-major index  */
+    uint8_t* tile_csc_Ptr;      /* numtile*16 (optional)                       */
+    uint8_t* tile_csc_Row;      /* nnz (optional)                              */
+    void* tile_csc_Val;         /* nnz (optional)                              */
+    /* scalar row view (CSR) of the same matrix */
+    int* row_ptr;               /* m+1                                         */
+    int* col_idx;               /* nnz                                         */
+    void* row_val;              /* nnz                                         */
+    void* priv;                 /* library private                             */
+} spg_tiles;
+
+/* Device-resident tile matrix C as steps 1-3 of src/spgemm_raw_v2.cu:111-243
+   produce it.  tile_nnzC is an int64 exclusive prefix (the reference's int
+   overflows beyond 2^31 nonzeros). */
+typedef struct {
+    int m, n;
+    int tilem, tilen;
+    int64_t numtileC;
+    int64_t nnzC;
+    spg_dtype dtype;
+    int* tile_ptrC;             /* tilem+1                                     */
+    int* tile_rowidxC;          /* numtileC                                    */
+    int* tile_colidxC;          /* numtileC                                    */
+    uint16_t* maskC;            /* numtileC*16                                 */
+    int64_t* tile_nnzC;         /* numtileC+1                                  */
+    uint8_t* ptrRowC;           /* numtileC*16                                 */
+    void* tile_valC;            /* nnzC                                        */
+    uint8_t* tile_colC;         /* nnzC, (r<<4)|c                              */
+    int64_t pairs;              /* matched tile pairs (filled by symbolic)     */
+    void* priv;
+} spg_ctiles;
+
+/* Per-call statistics of the last spg_symbolic / spg_numeric / spg_spgemm. */
+typedef struct {
+    float ms_step1;             /* C tile structure (count + scan + fill)      */
+    float ms_step2;             /* bitmask symbolic + scan + ptrRowC           */
+    float ms_step3;             /* numeric                                     */
+    int64_t products;           /* sum over A nonzeros of nnz(B row)           */
+    int64_t overflow_reruns;    /* pre-sized buffers that had to be re-run     */
+    int64_t work_items;         /* row-wise windows launched                   */
+    int64_t tensor_pairs;       /* tile pairs computed on tensor cores         */
+    int64_t fp64_tiles;         /* C tiles recomputed in FP64                  */
+} spg_stats;
+
+/* ---- handle ---------------------------------------------------------------
+ * Replaces: the implicit global state of main() (default stream, device
+ * selection) in src/spgemm_raw_v2.cu:61-71.  `stream` is a cudaStream_t (NULL =
+ * legacy default stream). */
+spg_status spg_create(spg_handle_t* h, int device, void* stream);
+spg_status spg_destroy(spg_handle_t h);
+spg_status spg_set_stream(spg_handle_t h, void* stream);
+const char* spg_last_error(spg_handle_t h);
+spg_status spg_get_stats(spg_handle_t h, spg_stats* out);
+
+/* ---- tiling ----------------------------------------------------------------
+ * Replaces csr2tile (src/tile_format.h:93-222), build_csc_tiles
+ * (src/tile_format.h:424-585) and upload_tiles (src/spgemm_raw_v2.cu:25-48).
+ * Input is a canonical CSR (columns strictly ascending within each row) in
+ * DEVICE memory; values are float (SPG_F32) or double (SPG_F64).  The result
+ * keeps a device copy of the CSR as its row view. */
+spg_status spg_tile_from_csr(spg_handle_t h, int m, int n, int64_t nnz, const int* d_row_ptr,
+                             const int* d_col_idx, const void* d_val, spg_dtype dtype,
+                             spg_layout layout, int flags, spg_tiles* out);
+
+/* Same, with the CSR in HOST memory (copied on the handle's stream). */
+spg_status spg_tile_from_csr_host(spg_handle_t h, int m, int n, int64_t nnz, const int* row_ptr,
+                                  const int* col_idx, const void* val, spg_dtype dtype,
+                                  spg_layout layout, int flags, spg_tiles* out);
+
+/* Replaces free_dev / free_tile_matrix (src/spgemm_raw_v2.cu:50-59,
+   src/tile_format.h:647-659). */
+spg_status spg_tiles_free(spg_handle_t h, spg_tiles* t);
+
+/* ---- SpGEMM steps ----------------------------------------------------------
+ * spg_symbolic replaces steps 1 and 2 of src/spgemm_raw_v2.cu:111-221
+ * (step1_count_kernel, ExclusiveSum, step1_fill_kernel, step2_symbolic_kernel,
+ * ExclusiveSum, step2_build_ptrRowC_kernel; src/spgemm_raw_kernels.cuh:23-215):
+ * fills tile_ptrC, tile_rowidxC, tile_colidxC, maskC, tile_nnzC, ptrRowC,
+ * numtileC and nnzC of *C and allocates tile_valC / tile_colC.
+ * A must be SPG_LAYOUT_ROW, B SPG_LAYOUT_B_CSC, A.n == B.m, same dtype. */
+spg_status spg_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                        spg_ctiles* C);
+
+/* Replaces step 3 (step3_numeric_kernel_v2, src/spgemm_raw_kernels_v2.cuh:10-139,
+ * launched at src/spgemm_raw_v2.cu:228-238): fills tile_valC and tile_colC. */
+spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                       spg_precision prec, spg_ctiles* C);
+
+/* Steps 1-3 in one call (the timed region of src/spgemm_raw_v2.cu:115-240). */
+spg_status spg_spgemm(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                      spg_precision prec, spg_ctiles* C);
+
+/* Copy C's arrays to host buffers sized from C->numtileC / C->nnzC (any
+   pointer may be NULL to skip that array).  tile_ptrC needs tilem+1 ints. */
+spg_status spg_ctiles_to_host(spg_handle_t h, const spg_ctiles* C, int* tile_ptrC, int* tile_rowidxC,
+                              int* tile_colidxC, uint16_t* maskC, int64_t* tile_nnzC,
+                              uint8_t* ptrRowC, void* tile_valC, uint8_t* tile_colC);
+
+/* Copy C tiles [tile_begin, tile_end) to host buffers indexed from 0: their
+   tile_rowidxC, tile_colidxC, maskC (16 per tile), ptrRowC (16 per tile), the
+   tile_end-tile_begin+1 entries of tile_nnzC starting at tile_begin (absolute
+   offsets), and the values / column bytes tile_nnzC[tile_begin] ..
+   tile_nnzC[tile_end]-1.  `val_capacity` is the number of values the value
+   and column buffers hold; SPG_ERR_INVALID (nothing copied) if the range holds
+   more.  *n_values receives the range's value count.  Lets a caller stream a C
+   larger than host memory (the reference reads C back whole,
+   src/spgemm_raw_v2.cu:257-266). */
+spg_status spg_ctiles_to_host_range(spg_handle_t h, const spg_ctiles* C, int64_t tile_begin, int64_t tile_end,
+                                    int* tile_rowidxC, int* tile_colidxC, uint16_t* maskC, int64_t* tile_nnzC,
+                                    uint8_t* ptrRowC, void* tile_valC, uint8_t* tile_colC, int64_t val_capacity,
+                                    int64_t* n_values);
+
+/* Copy a tile matrix's arrays to host buffers (NULL skips an array). */
+spg_status spg_tiles_to_host(spg_handle_t h, const spg_tiles* T, int* tile_ptr, int* tile_columnidx,
+                             int* tile_nnz, uint8_t* tile_csr_Ptr, uint16_t* mask, void* tile_csr_Val,
+                             uint8_t* tile_csr_Col, int* csc_tile_ptr, int* csc_tile_rowidx,
+                             uint8_t* tile_csc_Ptr, uint8_t* tile_csc_Row, void* tile_csc_Val);
+
+/* Replaces the free calls at src/spgemm_raw_v2.cu:361-367. */
+spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C);
+
+/* Intermediate products sum_{(i,k) in A} nnz(B(k,:)) (src/spgemm_raw_v2.cu:95-99),
+   computed on the device from the row views. */
+spg_status spg_products(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPGEMM_GB300_H */

@@ -1,0 +1,532 @@
+/*
+ * spgemm_oracle.c -- CPU restatement of the tiled SpGEMM hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA
+ * library in gpu_spgemm_gb300/csrc: tests, the smoke check and the CPU-baseline
+ * leg of bench.py call it; the product path never does.
+ *
+ * Every function restates one step of jianjianh1/GPU_SPGEMM (paths relative to
+ * that project):
+ *   orc_tile_count / orc_csr2tile      src/tile_format.h:93-222   (csr2tile)
+ *   orc_build_csc_tiles                src/tile_format.h:424-585  (build_csc_tiles)
+ *   orc_step1_count / orc_step1_fill   src/spgemm_raw_kernels.cuh:23-102
+ *   orc_step2_symbolic                 src/spgemm_raw_kernels.cuh:105-215
+ *   orc_step3_numeric                  src/spgemm_raw_kernels_v2.cuh:10-139
+ *   orc_tiles_to_csr                   src/spgemm_raw_v2.cu:268-284
+ *   orc_gustavson_*                    src/spgemm_raw_v2.cu:289-338
+ * Values are carried in double; the tile format arrays are bit-identical to the
+ * reference's for inputs in canonical CSR form (columns strictly ascending).
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define TS 16
+
+static int imin(int a, int b) { return a < b ? a : b; }
+
+static int cmp_int(const void* a, const void* b) {
+    int x = *(const int*)a, y = *(const int*)b;
+    return (x > y) - (x < y);
+}
+
+/* ------------------------------------------------------------------------ */
+/* csr2tile: src/tile_format.h:99-115 -- tiles per tile-row, prefix summed.  */
+/* tile_ptr has tilem+1 entries.  Returns numtile.                           */
+/* ------------------------------------------------------------------------ */
+int64_t orc_tile_count(int m, int n, const int* rp, const int* ci, int* tile_ptr) {
+    int tilem = (m + TS - 1) / TS, tilen = (n + TS - 1) / TS;
+    char* flag = (char*)calloc((size_t)tilen + 1, 1);
+    int* touched = (int*)malloc(sizeof(int) * ((size_t)tilen + 1));
+    tile_ptr[0] = 0;
+    for (int bi = 0; bi < tilem; bi++) {
+        int nt = 0, r0 = bi * TS, r1 = imin(r0 + TS, m);
+        for (int j = rp[r0]; j < rp[r1]; j++) {
+            int tc = ci[j] / TS;
+            if (!flag[tc]) { flag[tc] = 1; touched[nt++] = tc; }
+        }
+        for (int k = 0; k < nt; k++) flag[touched[k]] = 0;
+        tile_ptr[bi + 1] = tile_ptr[bi] + nt;
+    }
+    free(flag); free(touched);
+    return tile_ptr[tilem];
+}
+
+/* csr2tile: src/tile_format.h:117-215.  Arrays sized by orc_tile_count:     */
+/* tile_columnidx[numtile], tile_nnz[numtile+1] (prefix), tile_val[nnz],     */
+/* tile_col[nnz] packed (row<<4)|col, tile_ptrrow[numtile*16] (per-row       */
+/* exclusive offsets, uint8), mask[numtile*16] (bit 15-col set for col).     */
+void orc_csr2tile(int m, int n, const int* rp, const int* ci, const double* val,
+                  const int* tile_ptr, int* tile_columnidx, int* tile_nnz, double* tile_val,
+                  unsigned char* tile_col, unsigned char* tile_ptrrow, unsigned short* mask) {
+    int tilem = (m + TS - 1) / TS, tilen = (n + TS - 1) / TS;
+    int64_t numtile = tile_ptr[tilem];
+    char* flag = (char*)calloc((size_t)tilen + 1, 1);
+    int* touched = (int*)malloc(sizeof(int) * ((size_t)tilen + 1));
+    int* tc_to_t = (int*)malloc(sizeof(int) * ((size_t)tilen + 1));
+    int* cursor = (int*)calloc((size_t)numtile + 1, sizeof(int));
+    memset(tile_ptrrow, 0, (size_t)numtile * TS);
+    memset(mask, 0, sizeof(unsigned short) * (size_t)numtile * TS);
+    tile_nnz[0] = 0;
+    for (int bi = 0; bi < tilem; bi++) {
+        int nt = 0, r0 = bi * TS, r1 = imin(r0 + TS, m), base = tile_ptr[bi];
+        for (int j = rp[r0]; j < rp[r1]; j++) {
+            int tc = ci[j] / TS;
+            if (!flag[tc]) { flag[tc] = 1; touched[nt++] = tc; }
+        }
+        qsort(touched, nt, sizeof(int), cmp_int);
+        for (int k = 0; k < nt; k++) {
+            tile_columnidx[base + k] = touched[k];
+            tc_to_t[touched[k]] = base + k;
+            flag[touched[k]] = 0;
+        }
+        /* per (tile, row) counts */
+        for (int r = r0; r < r1; r++)
+            for (int j = rp[r]; j < rp[r + 1]; j++)
+                tile_ptrrow[(int64_t)tc_to_t[ci[j] / TS] * TS + (r - r0)]++;
+    }
+    /* nnz per tile, exclusive per-row scan (uint8 arithmetic as the reference) */
+    for (int64_t t = 0; t < numtile; t++) {
+        unsigned char* p = tile_ptrrow + t * TS;
+        unsigned char s = 0; int tot = 0;
+        for (int r = 0; r < TS; r++) { unsigned char v = p[r]; p[r] = s; s = (unsigned char)(s + v); tot += v; }
+        tile_nnz[t + 1] = tile_nnz[t] + tot;
+    }
+    /* values in CSR traversal order inside each tile (row-major) */
+    for (int bi = 0; bi < tilem; bi++) {
+        int r0 = bi * TS, r1 = imin(r0 + TS, m), base = tile_ptr[bi];
+        for (int k = base; k < tile_ptr[bi + 1]; k++) tc_to_t[tile_columnidx[k]] = k;
+        for (int r = r0; r < r1; r++)
+            for (int j = rp[r]; j < rp[r + 1]; j++) {
+                int tc = ci[j] / TS, lc = ci[j] - tc * TS, t = tc_to_t[tc];
+                int64_t dst = (int64_t)tile_nnz[t] + cursor[t]++;
+                tile_val[dst] = val[j];
+                tile_col[dst] = (unsigned char)(((r - r0) << 4) | lc);
+                mask[(int64_t)t * TS + (r - r0)] |= (unsigned short)(1u << (TS - 1 - lc));
+            }
+    }
+    free(flag); free(touched); free(tc_to_t); free(cursor);
+}
+
+/* ------------------------------------------------------------------------ */
+/* build_csc_tiles: src/tile_format.h:424-585.  B is re-tiled in CSC tile    */
+/* order (tiles sorted by tile column, then tile row); data inside a tile    */
+/* stays row-major with plain local columns.  numtile equals csr2tile's.     */
+/* Outputs: csc_tile_ptr[tilen+1], csc_tile_rowidx[numtile],                 */
+/* tile_nnz[numtile+1], tile_ptrrow[numtile*16], tile_val/tile_col[nnz],      */
+/* mask[numtile*16], and the in-tile CSC arrays tile_csc_ptr[numtile*16],    */
+/* tile_csc_row[nnz], tile_csc_val[nnz] (NULL to skip them).                 */
+/* ------------------------------------------------------------------------ */
+void orc_build_csc_tiles(int m, int n, const int* rp, const int* ci, const double* val,
+                         int* csc_tile_ptr, int* csc_tile_rowidx, int* tile_nnz,
+                         unsigned char* tile_ptrrow, double* tile_val, unsigned char* tile_col,
+                         unsigned short* mask, unsigned char* tile_csc_ptr,
+                         unsigned char* tile_csc_row, double* tile_csc_val) {
+    int tilem = (m + TS - 1) / TS, tilen = (n + TS - 1) / TS;
+    int nnz = rp[m];
+    /* element CSR -> CSC (stable: rows ascending inside a column) */
+    int* cp = (int*)calloc((size_t)n + 1, sizeof(int));
+    int* cr = (int*)malloc(sizeof(int) * ((size_t)nnz + 1));
+    double* cv = (double*)malloc(sizeof(double) * ((size_t)nnz + 1));
+    for (int j = 0; j < nnz; j++) cp[ci[j] + 1]++;
+    for (int c = 0; c < n; c++) cp[c + 1] += cp[c];
+    int* off = (int*)malloc(sizeof(int) * ((size_t)n + 1));
+    memcpy(off, cp, sizeof(int) * ((size_t)n + 1));
+    for (int r = 0; r < m; r++)
+        for (int j = rp[r]; j < rp[r + 1]; j++) { int p = off[ci[j]]++; cr[p] = r; cv[p] = val[j]; }
+    free(off);
+    /* tile rows present in each tile column, sorted */
+    char* flag = (char*)calloc((size_t)tilem + 1, 1);
+    int* touched = (int*)malloc(sizeof(int) * ((size_t)tilem + 1));
+    csc_tile_ptr[0] = 0;
+    for (int bt = 0; bt < tilen; bt++) {
+        int nt = 0, c0 = bt * TS, c1 = imin(c0 + TS, n);
+        for (int c = c0; c < c1; c++)
+            for (int j = cp[c]; j < cp[c + 1]; j++) {
+                int tr = cr[j] / TS;
+                if (!flag[tr]) { flag[tr] = 1; touched[nt++] = tr; }
+            }
+        qsort(touched, nt, sizeof(int), cmp_int);
+        for (int k = 0; k < nt; k++) { csc_tile_rowidx[csc_tile_ptr[bt] + k] = touched[k]; flag[touched[k]] = 0; }
+        csc_tile_ptr[bt + 1] = csc_tile_ptr[bt] + nt;
+    }
+    int64_t numtile = csc_tile_ptr[tilen];
+    int* tr_to_t = (int*)malloc(sizeof(int) * ((size_t)tilem + 1));
+    memset(tile_ptrrow, 0, (size_t)numtile * TS);
+    memset(mask, 0, sizeof(unsigned short) * (size_t)numtile * TS);
+    /* per (tile,row) counts */
+    for (int bt = 0; bt < tilen; bt++) {
+        int c0 = bt * TS, c1 = imin(c0 + TS, n);
+        for (int k = csc_tile_ptr[bt]; k < csc_tile_ptr[bt + 1]; k++) tr_to_t[csc_tile_rowidx[k]] = k;
+        for (int c = c0; c < c1; c++)
+            for (int j = cp[c]; j < cp[c + 1]; j++)
+                tile_ptrrow[(int64_t)tr_to_t[cr[j] / TS] * TS + (cr[j] % TS)]++;
+    }
+    tile_nnz[0] = 0;
+    for (int64_t t = 0; t < numtile; t++) {
+        unsigned char* p = tile_ptrrow + t * TS;
+        unsigned char s = 0; int tot = 0;
+        for (int r = 0; r < TS; r++) { unsigned char v = p[r]; p[r] = s; s = (unsigned char)(s + v); tot += v; }
+        tile_nnz[t + 1] = tile_nnz[t] + tot;
+    }
+    /* fill: traverse columns ascending so each tile row is column-sorted */
+    unsigned char* rowoff = (unsigned char*)calloc((size_t)numtile * TS + 1, 1);
+    for (int bt = 0; bt < tilen; bt++) {
+        int c0 = bt * TS, c1 = imin(c0 + TS, n);
+        for (int k = csc_tile_ptr[bt]; k < csc_tile_ptr[bt + 1]; k++) tr_to_t[csc_tile_rowidx[k]] = k;
+        for (int c = c0; c < c1; c++)
+            for (int j = cp[c]; j < cp[c + 1]; j++) {
+                int lr = cr[j] % TS, lc = c - c0, t = tr_to_t[cr[j] / TS];
+                int64_t dst = (int64_t)tile_nnz[t] + tile_ptrrow[(int64_t)t * TS + lr] + rowoff[(int64_t)t * TS + lr]++;
+                tile_val[dst] = cv[j];
+                tile_col[dst] = (unsigned char)lc;
+                mask[(int64_t)t * TS + lr] |= (unsigned short)(1u << (TS - 1 - lc));
+            }
+    }
+    free(rowoff);
+    /* in-tile CSC (src/tile_format.h:547-584): per-column offsets, local rows */
+    if (tile_csc_ptr && tile_csc_row && tile_csc_val) {
+        for (int64_t t = 0; t < numtile; t++) {
+            int base = tile_nnz[t], tn = tile_nnz[t + 1] - base;
+            unsigned char cnt[TS] = {0};
+            for (int e = 0; e < tn; e++) cnt[tile_col[base + e]]++;
+            unsigned char s = 0, co[TS];
+            for (int c = 0; c < TS; c++) { tile_csc_ptr[t * TS + c] = s; co[c] = s; s = (unsigned char)(s + cnt[c]); }
+            for (int r = 0; r < TS; r++) {
+                int rs = tile_ptrrow[t * TS + r];
+                int re = (r == TS - 1) ? tn : tile_ptrrow[t * TS + r + 1];
+                for (int e = rs; e < re; e++) {
+                    int lc = tile_col[base + e];
+                    int dst = base + co[lc]++;
+                    tile_csc_row[dst] = (unsigned char)r;
+                    tile_csc_val[dst] = tile_val[base + e];
+                }
+            }
+        }
+    }
+    free(cp); free(cr); free(cv); free(flag); free(touched); free(tr_to_t);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Step 1 (src/spgemm_raw_kernels.cuh:23-102): C tile-row i holds the union  */
+/* of B's (CSR-tiled) tile columns over A's tiles (i,k).  tile_ptrC[tilemA+1]*/
+/* is filled with the prefix; returns numtileC.                              */
+/* ------------------------------------------------------------------------ */
+int64_t orc_step1_count(int tilemA, int tilenB, const int* a_tile_ptr, const int* a_tile_col,
+                        const int* b_tile_ptr, const int* b_tile_col, int64_t* tile_ptrC) {
+    int64_t* cnt = (int64_t*)calloc((size_t)tilemA + 1, sizeof(int64_t));
+#pragma omp parallel
+    {
+        char* flag = (char*)calloc((size_t)tilenB + 1, 1);
+        int* touched = (int*)malloc(sizeof(int) * ((size_t)tilenB + 1));
+#pragma omp for schedule(dynamic, 16)
+        for (int i = 0; i < tilemA; i++) {
+            int nt = 0;
+            for (int a = a_tile_ptr[i]; a < a_tile_ptr[i + 1]; a++) {
+                int k = a_tile_col[a];
+                for (int b = b_tile_ptr[k]; b < b_tile_ptr[k + 1]; b++) {
+                    int j = b_tile_col[b];
+                    if (!flag[j]) { flag[j] = 1; touched[nt++] = j; }
+                }
+            }
+            for (int q = 0; q < nt; q++) flag[touched[q]] = 0;
+            cnt[i] = nt;
+        }
+        free(flag); free(touched);
+    }
+    tile_ptrC[0] = 0;
+    for (int i = 0; i < tilemA; i++) tile_ptrC[i + 1] = tile_ptrC[i] + cnt[i];
+    free(cnt);
+    return tile_ptrC[tilemA];
+}
+
+void orc_step1_fill(int tilemA, int tilenB, const int* a_tile_ptr, const int* a_tile_col,
+                    const int* b_tile_ptr, const int* b_tile_col, const int64_t* tile_ptrC,
+                    int* tile_rowidxC, int* tile_colidxC) {
+#pragma omp parallel
+    {
+        char* flag = (char*)calloc((size_t)tilenB + 1, 1);
+        int* touched = (int*)malloc(sizeof(int) * ((size_t)tilenB + 1));
+#pragma omp for schedule(dynamic, 16)
+        for (int i = 0; i < tilemA; i++) {
+            int nt = 0;
+            for (int a = a_tile_ptr[i]; a < a_tile_ptr[i + 1]; a++) {
+                int k = a_tile_col[a];
+                for (int b = b_tile_ptr[k]; b < b_tile_ptr[k + 1]; b++) {
+                    int j = b_tile_col[b];
+                    if (!flag[j]) { flag[j] = 1; touched[nt++] = j; }
+                }
+            }
+            qsort(touched, nt, sizeof(int), cmp_int);
+            for (int q = 0; q < nt; q++) {
+                flag[touched[q]] = 0;
+                tile_rowidxC[tile_ptrC[i] + q] = i;
+                tile_colidxC[tile_ptrC[i] + q] = touched[q];
+            }
+        }
+        free(flag); free(touched);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Step 2 (src/spgemm_raw_kernels.cuh:136-215).  For C tile (bi,bj) the      */
+/* matched pairs are A tiles (bi,k) and B CSC tiles (k,bj); row r of maskC   */
+/* is OR over pairs of OR over A's entries (r,kk) of maskB[kk].  Empty C      */
+/* tiles from step 1 stay with nnz 0.  Outputs maskC[numtileC*16],            */
+/* tile_nnzC[numtileC+1] as an exclusive prefix, ptrRowC[numtileC*16].        */
+/* Returns nnzC.  Also counts the matched pairs into *pairs_out if non-NULL. */
+/* ------------------------------------------------------------------------ */
+int64_t orc_step2_symbolic(int64_t numtileC, const int* tile_rowidxC, const int* tile_colidxC,
+                           const int* a_tile_ptr, const int* a_tile_col, const int* a_tile_nnz,
+                           const unsigned char* a_tile_colbyte, const unsigned char* a_tile_ptrrow,
+                           const int* b_csc_ptr, const int* b_csc_rowidx, const unsigned short* b_mask,
+                           unsigned short* maskC, int64_t* tile_nnzC, unsigned char* ptrRowC,
+                           int64_t* pairs_out) {
+    int64_t pairs = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : pairs)
+    for (int64_t t = 0; t < numtileC; t++) {
+        int bi = tile_rowidxC[t], bj = tile_colidxC[t];
+        int a = a_tile_ptr[bi], ae = a_tile_ptr[bi + 1];
+        int b = b_csc_ptr[bj], be = b_csc_ptr[bj + 1];
+        unsigned int rm[TS] = {0};
+        while (a < ae && b < be) {
+            int ka = a_tile_col[a], kb = b_csc_rowidx[b];
+            if (ka < kb) { a++; continue; }
+            if (kb < ka) { b++; continue; }
+            pairs++;
+            int s = a_tile_nnz[a], tn = a_tile_nnz[a + 1] - s;
+            for (int r = 0; r < TS; r++) {
+                int rs = a_tile_ptrrow[(int64_t)a * TS + r];
+                int re = (r == TS - 1) ? tn : a_tile_ptrrow[(int64_t)a * TS + r + 1];
+                for (int e = rs; e < re; e++)
+                    rm[r] |= b_mask[(int64_t)b * TS + (a_tile_colbyte[s + e] & 0xf)];
+            }
+            a++; b++;
+        }
+        int tot = 0;
+        unsigned char pr = 0;
+        for (int r = 0; r < TS; r++) {
+            maskC[t * TS + r] = (unsigned short)rm[r];
+            ptrRowC[t * TS + r] = pr;
+            int pc = __builtin_popcount(rm[r]);
+            pr = (unsigned char)(pr + pc);
+            tot += pc;
+        }
+        tile_nnzC[t + 1] = tot;
+    }
+    tile_nnzC[0] = 0;
+    for (int64_t t = 0; t < numtileC; t++) tile_nnzC[t + 1] += tile_nnzC[t];
+    if (pairs_out) *pairs_out = pairs;
+    return tile_nnzC[numtileC];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Step 3 (src/spgemm_raw_kernels_v2.cuh:69-136) in FP64 with a fixed        */
+/* summation order: pairs by ascending k, A entries in tile order, B entries */
+/* in tile order.  Output compaction is row-major with ascending column and  */
+/* tile_colC = (row<<4)|col.                                                  */
+/* ------------------------------------------------------------------------ */
+void orc_step3_numeric(int64_t numtileC, const int* tile_rowidxC, const int* tile_colidxC,
+                       const int* a_tile_ptr, const int* a_tile_col, const int* a_tile_nnz,
+                       const double* a_val, const unsigned char* a_colbyte, const unsigned char* a_ptrrow,
+                       const int* b_csc_ptr, const int* b_csc_rowidx, const int* b_tile_nnz,
+                       const double* b_val, const unsigned char* b_colbyte, const unsigned char* b_ptrrow,
+                       const int64_t* tile_nnzC, const unsigned short* maskC, const unsigned char* ptrRowC,
+                       double* valC, unsigned char* colC) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t t = 0; t < numtileC; t++) {
+        if (tile_nnzC[t + 1] == tile_nnzC[t]) continue;
+        int bi = tile_rowidxC[t], bj = tile_colidxC[t];
+        int a = a_tile_ptr[bi], ae = a_tile_ptr[bi + 1];
+        int b = b_csc_ptr[bj], be = b_csc_ptr[bj + 1];
+        double acc[TS * TS];
+        memset(acc, 0, sizeof(acc));
+        while (a < ae && b < be) {
+            int ka = a_tile_col[a], kb = b_csc_rowidx[b];
+            if (ka < kb) { a++; continue; }
+            if (kb < ka) { b++; continue; }
+            int as = a_tile_nnz[a], an = a_tile_nnz[a + 1] - as;
+            int bs = b_tile_nnz[b], bn = b_tile_nnz[b + 1] - bs;
+            for (int r = 0; r < TS; r++) {
+                int rs = a_ptrrow[(int64_t)a * TS + r];
+                int re = (r == TS - 1) ? an : a_ptrrow[(int64_t)a * TS + r + 1];
+                for (int e = rs; e < re; e++) {
+                    int k = a_colbyte[as + e] & 0xf;
+                    double va = a_val[as + e];
+                    int ks = b_ptrrow[(int64_t)b * TS + k];
+                    int ke = (k == TS - 1) ? bn : b_ptrrow[(int64_t)b * TS + k + 1];
+                    for (int f = ks; f < ke; f++) acc[r * TS + b_colbyte[bs + f]] += va * b_val[bs + f];
+                }
+            }
+            a++; b++;
+        }
+        int64_t base = tile_nnzC[t];
+        for (int r = 0; r < TS; r++) {
+            unsigned int mc = maskC[t * TS + r];
+            int64_t p = base + ptrRowC[t * TS + r];
+            for (int c = 0; c < TS; c++)
+                if ((mc >> (TS - 1 - c)) & 1u) {
+                    valC[p] = acc[r * TS + c];
+                    colC[p] = (unsigned char)((r << 4) | c);
+                    p++;
+                }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tile C -> CSR (src/spgemm_raw_v2.cu:268-284): entries outside m x n are   */
+/* dropped.  Two calls: row_ptr first (cols == NULL), then cols/vals.        */
+/* ------------------------------------------------------------------------ */
+void orc_tiles_to_csr(int m, int n, int64_t numtileC, const int* tile_rowidxC, const int* tile_colidxC,
+                      const int64_t* tile_nnzC, const unsigned char* colC, const double* valC,
+                      int64_t* row_ptr, int* cols, double* vals) {
+    if (!cols) {
+        memset(row_ptr, 0, sizeof(int64_t) * ((size_t)m + 1));
+        for (int64_t t = 0; t < numtileC; t++)
+            for (int64_t e = tile_nnzC[t]; e < tile_nnzC[t + 1]; e++) {
+                int r = tile_rowidxC[t] * TS + (colC[e] >> 4), c = tile_colidxC[t] * TS + (colC[e] & 0xf);
+                if (r < m && c < n) row_ptr[r + 1]++;
+            }
+        for (int r = 0; r < m; r++) row_ptr[r + 1] += row_ptr[r];
+        return;
+    }
+    int64_t* cur = (int64_t*)malloc(sizeof(int64_t) * ((size_t)m + 1));
+    memcpy(cur, row_ptr, sizeof(int64_t) * ((size_t)m + 1));
+    /* C tiles are sorted by (tile row, tile col), entries row-major inside a
+       tile, so walking tile rows then rows gives ascending columns. */
+    int64_t t0 = 0;
+    while (t0 < numtileC) {
+        int64_t t1 = t0;
+        while (t1 < numtileC && tile_rowidxC[t1] == tile_rowidxC[t0]) t1++;
+        for (int lr = 0; lr < TS; lr++)
+            for (int64_t t = t0; t < t1; t++)
+                for (int64_t e = tile_nnzC[t]; e < tile_nnzC[t + 1]; e++) {
+                    if ((colC[e] >> 4) != lr) continue;
+                    int r = tile_rowidxC[t] * TS + lr, c = tile_colidxC[t] * TS + (colC[e] & 0xf);
+                    if (r < m && c < n) { cols[cur[r]] = c; vals[cur[r]] = valC[e]; cur[r]++; }
+                }
+        t0 = t1;
+    }
+    free(cur);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Row-wise Gustavson (src/spgemm_raw_v2.cu:289-338): dense accumulator,     */
+/* used flags, sorted column list per row.  Structural: every column reached */
+/* by a product is kept, including exact cancellations.                      */
+/* orc_gustavson_rowcounts fills row_nnz[m]; orc_gustavson_fill writes cols  */
+/* and values at row_ptr (int64 prefix of row_nnz).  OpenMP over rows.       */
+/* ------------------------------------------------------------------------ */
+int64_t orc_gustavson_rowcounts(int m, int n, const int* arp, const int* aci,
+                                const int* brp, const int* bci, int64_t* row_nnz) {
+    int64_t total = 0;
+#pragma omp parallel reduction(+ : total)
+    {
+        int* mark = (int*)malloc(sizeof(int) * ((size_t)n + 1));
+        for (int c = 0; c < n; c++) mark[c] = -1;
+#pragma omp for schedule(dynamic, 64)
+        for (int i = 0; i < m; i++) {
+            int64_t cnt = 0;
+            for (int ja = arp[i]; ja < arp[i + 1]; ja++) {
+                int k = aci[ja];
+                for (int jb = brp[k]; jb < brp[k + 1]; jb++) {
+                    int c = bci[jb];
+                    if (mark[c] != i) { mark[c] = i; cnt++; }
+                }
+            }
+            row_nnz[i] = cnt;
+            total += cnt;
+        }
+        free(mark);
+    }
+    return total;
+}
+
+#define GUSTAVSON_FILL(NAME, T)                                                              \
+    void NAME(int m, int n, const int* arp, const int* aci, const T* av, const int* brp,      \
+              const int* bci, const T* bv, const int64_t* row_ptr, int* cci, T* cv) {         \
+        _Pragma("omp parallel") {                                                             \
+            T* acc = (T*)calloc((size_t)n + 1, sizeof(T));                                    \
+            char* used = (char*)calloc((size_t)n + 1, 1);                                     \
+            _Pragma("omp for schedule(dynamic, 64)") for (int i = 0; i < m; i++) {            \
+                int* cols = cci + row_ptr[i];                                                 \
+                int nc = 0;                                                                   \
+                for (int ja = arp[i]; ja < arp[i + 1]; ja++) {                                \
+                    int k = aci[ja];                                                          \
+                    T va = av[ja];                                                            \
+                    for (int jb = brp[k]; jb < brp[k + 1]; jb++) {                            \
+                        int c = bci[jb];                                                      \
+                        if (!used[c]) { used[c] = 1; cols[nc++] = c; }                        \
+                        acc[c] += va * bv[jb];                                                \
+                    }                                                                         \
+                }                                                                             \
+                qsort(cols, nc, sizeof(int), cmp_int);                                        \
+                for (int q = 0; q < nc; q++) {                                                \
+                    int c = cols[q];                                                          \
+                    cv[row_ptr[i] + q] = acc[c];                                              \
+                    acc[c] = 0; used[c] = 0;                                                  \
+                }                                                                             \
+            }                                                                                 \
+            free(acc); free(used);                                                            \
+        }                                                                                     \
+    }
+
+GUSTAVSON_FILL(orc_gustavson_fill_f64, double)
+GUSTAVSON_FILL(orc_gustavson_fill_f32, float)
+
+/* Gustavson restricted to rows [r0, r1) writing into caller scratch, for the
+   timed CPU baseline: one pass that forms every row (count + values) exactly
+   as a user-facing CPU SpGEMM must.  Returns the nnz produced. */
+#define GUSTAVSON_RANGE(NAME, T)                                                             \
+    int64_t NAME(int r0, int r1, int n, const int* arp, const int* aci, const T* av,          \
+                 const int* brp, const int* bci, const T* bv, int64_t* row_nnz) {             \
+        int64_t total = 0;                                                                    \
+        _Pragma("omp parallel reduction(+ : total)") {                                        \
+            T* acc = (T*)calloc((size_t)n + 1, sizeof(T));                                    \
+            char* used = (char*)calloc((size_t)n + 1, 1);                                     \
+            int* cols = (int*)malloc(sizeof(int) * ((size_t)n + 1));                          \
+            T sink = 0;                                                                       \
+            _Pragma("omp for schedule(dynamic, 64)") for (int i = r0; i < r1; i++) {          \
+                int nc = 0;                                                                   \
+                for (int ja = arp[i]; ja < arp[i + 1]; ja++) {                                \
+                    int k = aci[ja];                                                          \
+                    T va = av[ja];                                                            \
+                    for (int jb = brp[k]; jb < brp[k + 1]; jb++) {                            \
+                        int c = bci[jb];                                                      \
+                        if (!used[c]) { used[c] = 1; cols[nc++] = c; }                        \
+                        acc[c] += va * bv[jb];                                                \
+                    }                                                                         \
+                }                                                                             \
+                qsort(cols, nc, sizeof(int), cmp_int);                                        \
+                for (int q = 0; q < nc; q++) { sink += acc[cols[q]]; acc[cols[q]] = 0; used[cols[q]] = 0; } \
+                row_nnz[i - r0] = nc;                                                         \
+                total += nc;                                                                  \
+            }                                                                                 \
+            if (sink == (T)12345.678) total += 0; /* keep the accumulation live */            \
+            free(acc); free(used); free(cols);                                                \
+        }                                                                                     \
+        return total;                                                                         \
+    }
+
+GUSTAVSON_RANGE(orc_gustavson_range_f64, double)
+GUSTAVSON_RANGE(orc_gustavson_range_f32, float)
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_threads(int t) {
+#ifdef _OPENMP
+    if (t > 0) omp_set_num_threads(t);
+#else
+    (void)t;
+#endif
+}

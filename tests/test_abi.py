@@ -1,0 +1,76 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+include/*.h declares (no compute calls: these run without a GPU)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]+?\b(spg_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    d = _declared()
+    for must in ("spg_create", "spg_tile_from_csr", "spg_symbolic", "spg_numeric", "spg_spgemm"):
+        assert must in d
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from gpu_spgemm_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    from gpu_spgemm_gb300 import _lib
+    assert set(_declared()) <= set(_lib.SIGNATURES), set(_declared()) - set(_lib.SIGNATURES)
+
+
+def test_binding_struct_layout_matches_header():
+    # field order/types of spg_tiles / spg_ctiles mirror the header
+    from gpu_spgemm_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "spgemm_gb300.h")).read()
+    body = src[src.index("typedef struct {\n    int m, n;\n    int64_t nnz;"):src.index("} spg_tiles;")]
+    fields = re.findall(r"\*?\s*(\w+);", re.sub(r"/\*.*?\*/", "", body, flags=re.S))
+    flat = []
+    for line in re.sub(r"/\*.*?\*/", "", body, flags=re.S).splitlines()[1:]:
+        line = line.strip().rstrip(";")
+        if not line:
+            continue
+        decl = line.split(None, 1)[1] if " " in line else line
+        flat += [x.strip().lstrip("*") for x in decl.split(",")]
+    assert [f for f, _ in _lib.SpgTiles._fields_] == flat, (flat, fields)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    from gpu_spgemm_gb300 import _lib
+    with pytest.raises(RuntimeError):
+        _lib.load.__wrapped__(str(tmp_path / "nope.so")) if hasattr(_lib.load, "__wrapped__") else \
+            _lib_load_fresh(str(tmp_path / "nope.so"))
+
+
+def _lib_load_fresh(path):
+    from gpu_spgemm_gb300 import _lib
+    saved = _lib._lib
+    _lib._lib = None
+    try:
+        return _lib.load(path)
+    finally:
+        _lib._lib = saved

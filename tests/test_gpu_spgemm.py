@@ -1,0 +1,146 @@
+"""SpGEMM parity on the GPU: C's structure arrays bit-exact against the CPU
+oracle (itself pinned to the reference), values within the relative Frobenius
+tolerance against the FP64 oracle (FP64 path: 1e-12, FP32 path: 1e-6)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from gpu_spgemm_gb300 import api, synth
+import cases
+
+pytestmark = pytest.mark.gpu
+
+STRUCT_KEYS = ["tile_ptrC", "tile_rowidxC", "tile_colidxC", "maskC", "tile_nnzC", "ptrRowC", "tile_colC"]
+TOL = {np.float64: 1e-12, np.float32: 1e-6}
+
+
+def rel_frob(x, ref):
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    den = np.linalg.norm(ref)
+    return np.linalg.norm(x - ref) / (den if den > 0 else 1.0)
+
+
+def check_product(handle, a, b, algo, dtype, prec="f32"):
+    a = a.astype(dtype)
+    b = b.astype(dtype)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, b)
+    C = api.spgemm(handle, A, B, algo=algo, prec=prec)
+    got = C.to_host()
+    S = oracle.spgemm_tiles(a, b)
+    assert got["numtileC"] == S["numtileC"]
+    assert got["nnzC"] == S["nnzC"]
+    for k in STRUCT_KEYS:
+        np.testing.assert_array_equal(got[k], S[k].astype(got[k].dtype), err_msg=k)
+    err = rel_frob(got["tile_valC"], S["tile_valC"])
+    tol = TOL[np.float64] if (dtype == np.float64 or prec == "f64") else TOL[np.float32]
+    assert err <= tol, (err, tol)
+    assert got["pairs"] == S["pairs"]
+    return got, S
+
+
+@pytest.mark.parametrize("algo", ["plain", "rowwise"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("name,a,b", cases.product_cases(), ids=[c[0] for c in cases.product_cases()])
+def test_spgemm_small_cases(handle, name, a, b, dtype, algo):
+    check_product(handle, a, b, algo, dtype)
+
+
+@pytest.mark.parametrize("algo", ["plain", "rowwise"])
+def test_poisson2d_256_fp64_full_config(handle, algo):
+    a = synth.poisson2d(256)
+    got, S = check_product(handle, a, a, algo, np.float64)
+    assert got["numtileC"] == 50532 and got["nnzC"] == 846852
+
+
+@pytest.mark.parametrize("algo", ["plain", "rowwise"])
+@pytest.mark.parametrize("name,a", [("rmat_14", synth.rmat(14, 16)), ("stencil27_12", synth.stencil27_dof3(12)),
+                                    ("poisson3d_32", synth.poisson3d(32))])
+def test_medium_fp32(handle, name, a, algo):
+    check_product(handle, a, a, algo, np.float32)
+
+
+def test_pair_cache_overflow_rerun(handle, monkeypatch):
+    # shrink the matched-pair cache so step 2 overflows and re-runs; results unchanged
+    monkeypatch.setenv("SPG_SPEC_CAP_DIV", "64")
+    a = synth.stencil27_dof3(4, dtype=np.float64)
+    check_product(handle, a, a, "plain", np.float64)
+    assert handle.stats()["overflow_reruns"] >= 1
+
+
+def test_products_matches_host(handle):
+    a = synth.rmat(12, 8)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    assert api.products(handle, A, B) == synth.products(a, a)
+
+
+def test_dimension_mismatch_rejected(handle):
+    from gpu_spgemm_gb300._lib import SpgError
+    a = cases.random_csr(20, 30, 0.1, 1)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    with pytest.raises(SpgError):
+        api.spgemm(handle, A, B)
+
+
+def regions_case():
+    """A tile-row with > 16384 C tiles (several row-wise work items) and more
+    than 2048 A nonzeros (cursors in global scratch): a dense row in a
+    2^19-column matrix."""
+    n = 1 << 19
+    rng = np.random.Generator(np.random.PCG64(17))
+    rows = rng.integers(0, n, size=2 * n)
+    cols = rng.integers(0, n, size=2 * n)
+    rows = np.concatenate([rows, np.zeros(n, np.int64)])
+    cols = np.concatenate([cols, np.arange(n)])
+    key = np.unique(rows * n + cols)
+    r, c = key // n, key % n
+    rp = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(r, minlength=n), out=rp[1:])
+    return synth.CSR(n, n, rp.astype(np.int32), c.astype(np.int32), (rng.random(r.size) * 2 - 1).astype(np.float32))
+
+
+@pytest.mark.parametrize("algo", ["rowwise", "plain"])
+def test_multi_region_tile_row(handle, algo):
+    a = regions_case()
+    got, S = check_product(handle, a, a, algo, np.float32)
+    assert np.diff(S["tile_ptrC"]).max() > 16384
+
+
+@pytest.mark.parametrize("name,a", [("rmat_13", synth.rmat(13, 16)), ("stencil27_6", synth.stencil27_dof3(6))])
+def test_rowwise_fp64_accumulation_of_fp32(handle, name, a):
+    got, S = check_product(handle, a, a, "rowwise", np.float32, prec="f64")
+
+
+def test_host_range_copy_matches_full(handle):
+    import ctypes as C
+    from gpu_spgemm_gb300 import _lib as L
+    a = synth.rmat(12, 16)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    Cm = api.spgemm(handle, A, B)
+    full = Cm.to_host()
+    nt = Cm.numtileC
+    tb, te = nt // 3, (2 * nt) // 3
+    v0, v1 = full["tile_nnzC"][tb], full["tile_nnzC"][te]
+    o = dict(r=np.zeros(te - tb, np.int32), c=np.zeros(te - tb, np.int32), m=np.zeros((te - tb) * 16, np.uint16),
+             p=np.zeros(te - tb + 1, np.int64), pr=np.zeros((te - tb) * 16, np.uint8),
+             v=np.zeros(v1 - v0, np.float32), cc=np.zeros(v1 - v0, np.uint8))
+    nv = C.c_int64()
+    P = lambda x: x.ctypes.data_as(C.c_void_p)
+    handle.check(handle.lib.spg_ctiles_to_host_range(handle.h, C.byref(Cm.c), tb, te, P(o["r"]), P(o["c"]),
+                                                     P(o["m"]), P(o["p"]), P(o["pr"]), P(o["v"]), P(o["cc"]),
+                                                     int(v1 - v0), C.byref(nv)))
+    assert nv.value == v1 - v0
+    np.testing.assert_array_equal(o["r"], full["tile_rowidxC"][tb:te])
+    np.testing.assert_array_equal(o["m"], full["maskC"][tb * 16:te * 16])
+    np.testing.assert_array_equal(o["p"], full["tile_nnzC"][tb:te + 1])
+    np.testing.assert_array_equal(o["v"], full["tile_valC"][v0:v1])
+    np.testing.assert_array_equal(o["cc"], full["tile_colC"][v0:v1])
+    st = handle.lib.spg_ctiles_to_host_range(handle.h, C.byref(Cm.c), tb, te, None, None, None, None, None,
+                                             P(o["v"]), None, int(v1 - v0) - 1, C.byref(nv))
+    assert st == L.SPG_ERR_INVALID
