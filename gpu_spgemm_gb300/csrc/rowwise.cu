@@ -33,7 +33,9 @@ constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
 constexpr int NW_MAXT = 1024;   // C tiles per numeric window
 constexpr int NW_VALS = 8192;   // C values per numeric window
-constexpr int MAXA_SMEM = 2048; // A nonzeros per tile-row whose cursors fit in shared memory
+constexpr int MAXA_SMEM = 1024; // A nonzeros per tile-row whose cursors fit in shared memory
+constexpr int SHORT = 8;        // B entries a lane handles alone before handing a segment to a warp
+constexpr int LONG_CAP = 512;   // segments queued for warp-cooperative processing per pass
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
     while (lo < hi) {
@@ -153,10 +155,75 @@ __device__ __forceinline__ int row_of(const int* s_rows, int e) {
     return r;
 }
 
+// Runs `op(x, r, p, c)` for every B entry (position p, column c < limit) that
+// the A nonzeros of the tile-row reach inside the current window, advancing
+// each nonzero's cursor past the window.  One lane per A nonzero walks up to
+// SHORT entries of its B row alone (R-MAT: most (nonzero, window) visits hold
+// one or two products); longer segments are queued and finished by a whole
+// warp, 32 entries per step.  `op` is called with the A-nonzero index x.
+template <typename Op>
+__device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const int* s_rows, int limit,
+                                            const int* __restrict__ a_ci, const int* __restrict__ b_rp,
+                                            const int* __restrict__ b_ci, int2* s_long, int* s_nlong, Op op) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    while (true) {
+        if (tid == 0) *s_nlong = 0;
+        __syncthreads();
+        int pending = 0;
+        for (int x = tid; x < it.na; x += RW_THREADS) {
+            const int2 cs = cur[x];
+            if (cs.y >= limit) continue;
+            const int e = it.e0 + x;
+            const int k = __ldg(&a_ci[e]);
+            const int be = __ldg(&b_rp[k + 1]);
+            const int r = row_of(s_rows, e);
+            int p = cs.x, c = cs.y, cnt = 0;
+            while (c < limit && cnt < SHORT) {
+                op(x, r, p, c);
+                p++;
+                cnt++;
+                c = p < be ? __ldg(&b_ci[p]) : INT_MAX;
+            }
+            if (c < limit) {
+                const int slot = atomicAdd(s_nlong, 1);
+                if (slot < LONG_CAP) s_long[slot] = make_int2(x, p);
+                else pending = 1;
+            }
+            cur[x] = make_int2(p, c);
+        }
+        __syncthreads();
+        const int nl = min(*s_nlong, LONG_CAP);
+        for (int y = warp; y < nl; y += RW_WARPS) {
+            const int x = s_long[y].x;
+            const int e = it.e0 + x;
+            const int k = __ldg(&a_ci[e]);
+            const int be = __ldg(&b_rp[k + 1]);
+            const int r = row_of(s_rows, e);
+            int p = s_long[y].y, nextc = INT_MAX;
+            while (true) {
+                const int q = p + lane;
+                const int c = q < be ? __ldg(&b_ci[q]) : INT_MAX;
+                const bool in = c < limit;
+                const unsigned bal = __ballot_sync(0xffffffffu, in);
+                if (in) op(x, r, q, c);
+                const int n_in = __popc(bal);
+                if (n_in < 32) {
+                    nextc = __shfl_sync(0xffffffffu, c, n_in);
+                    p += n_in;
+                    break;
+                }
+                p += 32;
+            }
+            if (lane == 0) cur[x] = make_int2(p, nextc);
+        }
+        if (!__syncthreads_or(pending)) break;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // symbolic
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(RW_THREADS)
+__global__ void __launch_bounds__(RW_THREADS, 2)
 rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t nitems,
                    const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                    const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
@@ -170,7 +237,9 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ int2 s_long[LONG_CAP];
+    __shared__ int s_nlong;
+    const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
@@ -183,35 +252,12 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
-            for (int x = warp; x < it.na; x += RW_WARPS) {
-                const int2 cs = cur[x];
-                if (cs.y >= limit) continue;
-                const int e = it.e0 + x;
-                const int k = __ldg(&a_ci[e]);
-                const int be = __ldg(&b_rp[k + 1]);
-                const int r = row_of(s_rows, e);
-                int p = cs.x, nextc = INT_MAX;
-                while (true) {
-                    const int qq = p + lane;
-                    const int c = qq < be ? __ldg(&b_ci[qq]) : INT_MAX;
-                    const bool in = c < limit;
-                    const unsigned bal = __ballot_sync(0xffffffffu, in);
-                    if (in) {
-                        const int lt = wrank(bm, pre, wlo, c >> 4);
-                        const int idx = r * WS + lt;
-                        atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
-                    }
-                    const int cnt = __popc(bal);
-                    if (cnt < 32) {
-                        nextc = __shfl_sync(0xffffffffu, c, cnt);
-                        p += cnt;
-                        break;
-                    }
-                    p += 32;
-                }
-                if (lane == 0) cur[x] = make_int2(p, nextc);
-            }
-            __syncthreads();
+            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, s_long, &s_nlong,
+                        [&](int, int r, int, int c) {
+                            const int lt = wrank(bm, pre, wlo, c >> 4);
+                            const int idx = r * WS + lt;
+                            atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
+                        });
             for (int x = tid; x < nt; x += RW_THREADS) {
                 uint32_t mw[8];
                 uint32_t pw[4] = {0u, 0u, 0u, 0u};
@@ -243,7 +289,7 @@ template <typename ACC>
 __device__ __forceinline__ void acc_add(ACC* a, ACC v) { atomicAdd(a, v); }
 
 template <typename V, typename ACC>
-__global__ void __launch_bounds__(RW_THREADS)
+__global__ void __launch_bounds__(RW_THREADS, 2)
 rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t nitems,
                   const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                   const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
@@ -263,7 +309,9 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
     __shared__ int s_nt;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ int2 s_long[LONG_CAP];
+    __shared__ int s_nlong;
+    const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
@@ -302,36 +350,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
-            for (int x = warp; x < it.na; x += RW_WARPS) {
-                const int2 cs = cur[x];
-                if (cs.y >= limit) continue;
-                const int e = it.e0 + x;
-                const int k = __ldg(&a_ci[e]);
-                const ACC va = (ACC)__ldg(&a_val[e]);
-                const int be = __ldg(&b_rp[k + 1]);
-                const int r = row_of(s_rows, e);
-                int p = cs.x, nextc = INT_MAX;
-                while (true) {
-                    const int qq = p + lane;
-                    const int c = qq < be ? __ldg(&b_ci[qq]) : INT_MAX;
-                    const bool in = c < limit;
-                    const unsigned bal = __ballot_sync(0xffffffffu, in);
-                    if (in) {
-                        const int lt = wrank(bm, pre, wlo, c >> 4);
-                        const uint32_t m16 = mk[lt * TS + r];
-                        const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
-                        acc_add(&acc[pos], va * (ACC)__ldg(&b_val[qq]));
-                    }
-                    const int cnt = __popc(bal);
-                    if (cnt < 32) {
-                        nextc = __shfl_sync(0xffffffffu, c, cnt);
-                        p += cnt;
-                        break;
-                    }
-                    p += 32;
-                }
-                if (lane == 0) cur[x] = make_int2(p, nextc);
-            }
+            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, s_long, &s_nlong,
+                        [&](int x, int r, int p, int c) {
+                            const int lt = wrank(bm, pre, wlo, c >> 4);
+                            const uint32_t m16 = mk[lt * TS + r];
+                            const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
+                            acc_add(&acc[pos], (ACC)__ldg(&a_val[it.e0 + x]) * (ACC)__ldg(&b_val[p]));
+                        });
             __syncthreads();
             for (int x = tid; x < nv; x += RW_THREADS) valC[v0 + x] = (V)acc[x];
             for (int x = tid; x < ntw * TS; x += RW_THREADS) {
@@ -389,17 +414,9 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, spg_ctiles* C, 
     int64_t mx = 0;
     SPG_TRY(spg_read_i64(h, (const int64_t*)(rp->counters + 2), &mx));
     rp->max_na = (int)mx;
-    // persistent grid: as many CTAs as fit (numeric is the larger footprint)
-    int occ = 0;
-    const int nwords_b = (C->tilen + 31) / 32;
-    const size_t smem = num_smem<double>(nwords_b) > sym_smem(nwords_b) ? num_smem<double>(nwords_b)
-                                                                         : sym_smem(nwords_b);
-    SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<double, double>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_numeric_kernel<double, double>, RW_THREADS,
-                                                              smem));
-    if (occ < 1) occ = 1;
-    rp->grid = h->num_sms * occ * 2;
+    // cursor scratch for tile-rows with more A nonzeros than fit in shared
+    // memory: one slice per resident CTA (<= 4 CTAs of 512 threads per SM)
+    rp->grid = h->num_sms * 4;
     if (rp->max_na > MAXA_SMEM) {
         SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na + 1));
     }
@@ -416,7 +433,10 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise symbolic: B too wide");
     SPG_CUDA(h, cudaFuncSetAttribute(rw_symbolic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters, 0, sizeof(unsigned long long), h->stream));
-    rw_symbolic_kernel<<<rp->grid, RW_THREADS, smem, h->stream>>>(
+    int occ = 1;
+    SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_symbolic_kernel, RW_THREADS, smem));
+    const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
+    rw_symbolic_kernel<<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, A->row_ptr,
         A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na);
     SPG_CUDA(h, cudaGetLastError());
@@ -432,7 +452,10 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
     SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<V, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters + 1, 0, sizeof(unsigned long long), h->stream));
-    rw_numeric_kernel<V, ACC><<<rp->grid, RW_THREADS, smem, h->stream>>>(
+    int occ = 1;
+    SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_numeric_kernel<V, ACC>, RW_THREADS, smem));
+    const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
+    rw_numeric_kernel<V, ACC><<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
         (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na);

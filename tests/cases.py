@@ -92,3 +92,11 @@ def product_cases():
         ("poisson*empty", synth.poisson2d(4), empty_csr(16, 16)),
         ("rmat_9*transpose", rm, synth.transpose(rm)),
     ]
+
+
+def reference_kernel_extra_cases():
+    """Extra cases for the reference-kernel fixtures: C tiles with more than 32
+    matched tile pairs (the merge fallback of src/spgemm_raw_kernels.cuh:189-194
+    and src/spgemm_raw_kernels_v2.cuh:100-109)."""
+    a = random_csr(600, 600, 0.015, 31)
+    return [("rand_600_many_pairs^2", a, a)]
