@@ -259,8 +259,11 @@ def run_ours(args):
     dom_bytes = {"step1": 4 * (A.tilem + 1) * 2 + 4 * A.numtile + 4 * B.numtile + 8 * numtileC,
                  "step2": sym_bytes, "step3": num_bytes}[dom]
     achieved = dom_bytes / (steps_ms[dom] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": {"step1": "c1_count/fill", "step2": "c2_symbolic",
-                                           "step3": "c3_numeric"}[dom] if args.algo != "rowwise" else dom,
+    rowwise = stats[-1].get("algo_used", 1) == 2
+    names = {"step1": "c1_count_kernel + c1_fill_kernel",
+             "step2": "rw_symbolic_kernel" if rowwise else "c2_symbolic_kernel",
+             "step3": "rw_numeric_kernel" if rowwise else "c3_numeric_kernel"}
+    roofline = {"bound": "hbm", "kernel": names[dom],
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "peak_source": peak_src, "algorithmic_bytes": dom_bytes, "ms": steps_ms[dom],
                 "traffic": args.traffic}

@@ -45,7 +45,7 @@ class SpgCTiles(C.Structure):
 class SpgStats(C.Structure):
     _fields_ = [("ms_step1", C.c_float), ("ms_step2", C.c_float), ("ms_step3", C.c_float),
                 ("products", I64), ("overflow_reruns", I64), ("work_items", I64), ("tensor_pairs", I64),
-                ("fp64_tiles", I64)]
+                ("fp64_tiles", I64), ("algo_used", I32), ("reserved", I32)]
 
 
 # name -> (restype, argtypes); every symbol the header declares
@@ -67,6 +67,10 @@ SIGNATURES = {
     "spg_tiles_to_host": (I32, [P, C.POINTER(SpgTiles), P, P, P, P, P, P, P, P, P, P, P, P]),
     "spg_ctiles_free": (I32, [P, C.POINTER(SpgCTiles)]),
     "spg_products": (I32, [P, C.POINTER(SpgTiles), C.POINTER(SpgTiles), C.POINTER(I64)]),
+    "spg_csr_transpose": (I32, [P, I32, I32, I64, P, P, P, I32, P, P, P]),
+    "spg_ctiles_to_csr": (I32, [P, C.POINTER(SpgCTiles), P, P, P, C.POINTER(I64)]),
+    "spg_galerkin": (I32, [P, I32, I32, I64, P, P, P, I64, P, P, P, I32, I32, I32, C.POINTER(SpgCTiles),
+                           C.POINTER(I64)]),
 }
 
 _lib = None

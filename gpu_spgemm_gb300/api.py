@@ -227,3 +227,71 @@ def products(handle: Handle, A: TileMatrix, B: TileMatrix) -> int:
     out = C.c_int64()
     handle.check(handle.lib.spg_products(handle.h, C.byref(A.t), C.byref(B.t), C.byref(out)))
     return out.value
+
+
+# ---------------------------------------------------------------------------
+# conversions and chained products (device memory for outputs comes from torch,
+# used only as a device allocator here)
+# ---------------------------------------------------------------------------
+def _torch_empty(n, dtype):
+    import torch
+    return torch.empty(max(int(n), 1), dtype=dtype, device="cuda")
+
+
+def transpose(handle: Handle, T: TileMatrix, layout: str = "b_csc") -> TileMatrix:
+    """Tile the transpose of T (from T's device row view): the device form of
+    the reference's --aat transpose (src/spgemm_raw_v2.cu:79-90)."""
+    import torch
+    t = T.t
+    vt = torch.float64 if t.dtype == L.SPG_F64 else torch.float32
+    rp = _torch_empty(t.n + 1, torch.int32)
+    ci = _torch_empty(t.nnz, torch.int32)
+    vv = _torch_empty(t.nnz, vt)
+    handle.check(handle.lib.spg_csr_transpose(handle.h, t.m, t.n, t.nnz, C.c_void_p(t.row_ptr), C.c_void_p(t.col_idx),
+                                              C.c_void_p(t.row_val), t.dtype, C.c_void_p(rp.data_ptr()),
+                                              C.c_void_p(ci.data_ptr()), C.c_void_p(vv.data_ptr())))
+    lay = L.SPG_LAYOUT_B_CSC if layout == "b_csc" else L.SPG_LAYOUT_ROW
+    out = L.SpgTiles()
+    handle.check(handle.lib.spg_tile_from_csr(handle.h, t.n, t.m, t.nnz, C.c_void_p(rp.data_ptr()),
+                                              C.c_void_p(ci.data_ptr()), C.c_void_p(vv.data_ptr()), t.dtype, lay, 0,
+                                              C.byref(out)))
+    return TileMatrix(handle, out)
+
+
+def ctiles_to_csr(handle: Handle, Cm: CTileMatrix):
+    """C's tiles -> host CSR arrays (row_ptr int32, col_idx int32, values),
+    expanded on the device (src/spgemm_raw_v2.cu:268-284)."""
+    import torch
+    c = Cm.c
+    nnz = C.c_int64()
+    handle.check(handle.lib.spg_ctiles_to_csr(handle.h, C.byref(c), None, None, None, C.byref(nnz)))
+    vt = torch.float64 if c.dtype == L.SPG_F64 else torch.float32
+    rp = _torch_empty(c.m + 1, torch.int32)
+    ci = _torch_empty(nnz.value, torch.int32)
+    vv = _torch_empty(nnz.value, vt)
+    handle.check(handle.lib.spg_ctiles_to_csr(handle.h, C.byref(c), C.c_void_p(rp.data_ptr()),
+                                              C.c_void_p(ci.data_ptr()), C.c_void_p(vv.data_ptr()), C.byref(nnz)))
+    torch.cuda.synchronize()
+    n = nnz.value
+    return rp.cpu().numpy()[:c.m + 1], ci.cpu().numpy()[:n], vv.cpu().numpy()[:n]
+
+
+def galerkin(handle: Handle, a, p, algo: str = "auto", prec: str = "f32"):
+    """RAP = P^T (A P) for host CSR A (m x m) and P (m x nc); returns
+    (CTileMatrix, intermediate products of both SpGEMMs)."""
+    import torch
+    dev = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    ar, ac, av = dev(a.row_ptr.astype(np.int32)), dev(a.col_idx.astype(np.int32)), dev(a.val)
+    pr_, pc, pv = dev(p.row_ptr.astype(np.int32)), dev(p.col_idx.astype(np.int32)), dev(p.val)
+    return galerkin_device(handle, a.m, p.n, a.nnz, ar.data_ptr(), ac.data_ptr(), av.data_ptr(), p.nnz,
+                           pr_.data_ptr(), pc.data_ptr(), pv.data_ptr(), a.val.dtype, algo, prec, keep=(ar, ac, av, pr_, pc, pv))
+
+
+def galerkin_device(handle: Handle, m, nc, nnza, a_rp, a_ci, a_val, nnzp, p_rp, p_ci, p_val, dtype,
+                    algo="auto", prec="f32", keep=None):
+    c = L.SpgCTiles()
+    prod = C.c_int64()
+    handle.check(handle.lib.spg_galerkin(handle.h, m, nc, nnza, C.c_void_p(a_rp), C.c_void_p(a_ci), C.c_void_p(a_val),
+                                         nnzp, C.c_void_p(p_rp), C.c_void_p(p_ci), C.c_void_p(p_val),
+                                         _dtype_code(dtype), _ALGOS[algo], _PRECS[prec], C.byref(c), C.byref(prod)))
+    return CTileMatrix(handle, c), prod.value

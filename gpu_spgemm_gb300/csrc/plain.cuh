@@ -22,3 +22,6 @@ spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
 
 spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int* d_rp, const int* d_ci,
                            const void* d_val, spg_dtype dtype, spg_layout layout, int flags, spg_tiles* out);
+
+spg_status ctiles_to_csr_impl(spg_handle_t h, const spg_ctiles* C, int* out_rp, int* out_ci, void* out_val,
+                              int64_t* nnz_out);

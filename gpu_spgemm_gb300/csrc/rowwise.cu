@@ -45,21 +45,57 @@ __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, 
     return lo;
 }
 
+// Plan, pass 1: per C tile-row its products (sum over A's nonzeros of the B
+// row lengths), the largest A nonzero count of any tile-row with C tiles, and
+// the total products.  One warp per tile-row.
 __global__ void rw_plan_kernel(int tilem, int m, const int* __restrict__ tile_ptrC, const int* __restrict__ a_rp,
-                               int64_t* __restrict__ nitems, unsigned long long* __restrict__ max_na) {
-    unsigned long long mx = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
+                               const int* __restrict__ a_ci, const int* __restrict__ b_rp,
+                               int64_t* __restrict__ prod, unsigned long long* __restrict__ max_na,
+                               unsigned long long* __restrict__ total) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < tilem; i += nw) {
         const int ntc = tile_ptrC[i + 1] - tile_ptrC[i];
-        nitems[i] = ntc > 0 ? (ntc + RT - 1) / RT : 0;
-        const int na = a_rp[min(i * TS + TS, m)] - a_rp[i * TS];
-        if (ntc > 0 && (unsigned long long)na > mx) mx = (unsigned long long)na;
+        const int e0 = a_rp[i * TS], e1 = a_rp[min(i * TS + TS, m)];
+        unsigned long long p = 0;
+        if (ntc > 0)
+            for (int e = e0 + lane; e < e1; e += 32) {
+                const int k = __ldg(&a_ci[e]);
+                p += (unsigned long long)(__ldg(&b_rp[k + 1]) - __ldg(&b_rp[k]));
+            }
+        p = warp_sum(p);
+        if (lane == 0) {
+            prod[i] = (int64_t)p;
+            if (ntc > 0) {
+                atomicMax(max_na, (unsigned long long)(e1 - e0));
+                if (p) atomicAdd(total, p);
+            }
+        }
     }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, d);
-        mx = o > mx ? o : mx;
+}
+
+// Plan, pass 2: work items per tile-row.  A tile-row is cut into regions of
+// at most RT C tiles and at most ~PW products, PW = total / (SMs * 16) (at
+// least 2^16): hub tile-rows of a power-law matrix become many balanced
+// items instead of one long one.
+__global__ void rw_plan2_kernel(int tilem, int num_sms, const int* __restrict__ tile_ptrC,
+                                const int64_t* __restrict__ prod, const unsigned long long* __restrict__ total,
+                                int64_t* __restrict__ nitems) {
+    const unsigned long long tot = *total;
+    unsigned long long pw = tot / ((unsigned long long)num_sms * 16ull);
+    if (pw < (1ull << 16)) pw = 1ull << 16;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
+        const int64_t ntc = tile_ptrC[i + 1] - tile_ptrC[i];
+        int64_t n = 0;
+        if (ntc > 0) {
+            const int64_t by_t = (ntc + RT - 1) / RT;
+            const int64_t by_p = (int64_t)(((unsigned long long)prod[i] + pw - 1) / pw);
+            n = by_t > by_p ? by_t : by_p;
+            if (n > ntc) n = ntc;
+            if (n < 1) n = 1;
+        }
+        nitems[i] = n;
     }
-    if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_na, mx);
 }
 
 // Shared state of one work item.
@@ -82,12 +118,13 @@ __device__ bool next_item(unsigned long long* ticket, const int64_t* __restrict_
             const int mid = (lo + hi) >> 1;
             if (item_prefix[mid] <= item) lo = mid; else hi = mid;
         }
-        const int q = (int)(item - item_prefix[lo]);
-        const int ts = tile_ptrC[lo], te = tile_ptrC[lo + 1];
+        const int64_t q = item - item_prefix[lo];
+        const int64_t nreg = item_prefix[lo + 1] - item_prefix[lo];
+        const int64_t ts = tile_ptrC[lo], ntc = tile_ptrC[lo + 1] - ts;
         s_it->i = lo;
-        s_it->q = q;
-        s_it->rs = ts + q * RT;
-        s_it->re = min(ts + (q + 1) * RT, te);
+        s_it->q = (int)q;
+        s_it->rs = (int)(ts + (q * ntc) / nreg);
+        s_it->re = (int)(ts + ((q + 1) * ntc) / nreg);
     }
     __syncthreads();
     if (threadIdx.x <= TS) {
@@ -394,26 +431,36 @@ spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B) 
     return SPG_ALGO_ROWWISE;
 }
 
-static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, spg_ctiles* C, RowwisePriv* rp) {
+static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                             RowwisePriv* rp) {
     if (rp->item_prefix) return SPG_OK;
     const int tilem = C->tilem;
     int64_t* nit = nullptr;
+    int64_t* prod = nullptr;
     SPG_TRY(spg_alloc_t(h, &nit, (size_t)tilem + 1));
+    SPG_TRY(spg_alloc_t(h, &prod, (size_t)tilem + 1));
     SPG_TRY(spg_alloc_t(h, &rp->item_prefix, (size_t)tilem + 1));
     SPG_TRY(spg_alloc_t(h, &rp->counters, 4));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters, 0, 4 * sizeof(unsigned long long), h->stream));
     if (tilem > 0) {
-        int g = (int)ceil_div(tilem, 256);
+        int g = (int)ceil_div((int64_t)tilem * 32, 256);
         if (g > h->num_sms * 8) g = h->num_sms * 8;
-        rw_plan_kernel<<<g, 256, 0, h->stream>>>(tilem, A->m, C->tile_ptrC, A->row_ptr, nit, rp->counters + 2);
+        rw_plan_kernel<<<g, 256, 0, h->stream>>>(tilem, A->m, C->tile_ptrC, A->row_ptr, A->col_idx, B->row_ptr, prod,
+                                                 rp->counters + 2, rp->counters + 3);
+        SPG_CUDA(h, cudaGetLastError());
+        int g2 = (int)ceil_div(tilem, 256);
+        if (g2 > h->num_sms * 8) g2 = h->num_sms * 8;
+        rw_plan2_kernel<<<g2, 256, 0, h->stream>>>(tilem, h->num_sms, C->tile_ptrC, prod, rp->counters + 3, nit);
         SPG_CUDA(h, cudaGetLastError());
     }
     SPG_TRY(spg_scan_i64_to_i64(h, nit, rp->item_prefix, tilem));
     spg_free_async(h, nit);
+    spg_free_async(h, prod);
     SPG_TRY(spg_read_i64(h, rp->item_prefix + tilem, &rp->nitems));
     int64_t mx = 0;
     SPG_TRY(spg_read_i64(h, (const int64_t*)(rp->counters + 2), &mx));
     rp->max_na = (int)mx;
+    SPG_TRY(spg_read_i64(h, (const int64_t*)(rp->counters + 3), &h->stats.products));
     // cursor scratch for tile-rows with more A nonzeros than fit in shared
     // memory: one slice per resident CTA (<= 4 CTAs of 512 threads per SM)
     rp->grid = h->num_sms * 4;
@@ -426,7 +473,7 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, spg_ctiles* C, 
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
                             int* tile_cnt) {
     if (C->numtileC == 0) return SPG_OK;
-    SPG_TRY(rw_prepare(h, A, C, rp));
+    SPG_TRY(rw_prepare(h, A, B, C, rp));
     h->stats.work_items = rp->nitems;
     const int nwords_b = (B->tilen + 31) / 32;
     const size_t smem = sym_smem(nwords_b);
@@ -466,7 +513,7 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
 spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
                            spg_precision prec) {
     if (C->numtileC == 0 || C->nnzC == 0) return SPG_OK;
-    SPG_TRY(rw_prepare(h, A, C, rp));
+    SPG_TRY(rw_prepare(h, A, B, C, rp));
     if (A->dtype == SPG_F64) return launch_numeric<double, double>(h, A, B, C, rp);
     if (prec == SPG_PREC_F64) return launch_numeric<float, double>(h, A, B, C, rp);
     return launch_numeric<float, float>(h, A, B, C, rp);

@@ -171,7 +171,21 @@ radix_scatter_kernel(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, u
     }
 }
 
+__global__ void iota_u32_kernel(uint32_t* v, int64_t n) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        v[t] = (uint32_t)t;
+}
+
 }  // namespace
+
+spg_status spg_iota_u32(spg_handle_t h, uint32_t* v, int64_t n) {
+    if (n <= 0) return SPG_OK;
+    int64_t g = ceil_div(n, 256);
+    if (g > (int64_t)h->num_sms * 16) g = (int64_t)h->num_sms * 16;
+    iota_u32_kernel<<<(int)g, 256, 0, h->stream>>>(v, n);
+    SPG_CUDA(h, cudaGetLastError());
+    return SPG_OK;
+}
 
 spg_status spg_scan_i32_to_i32(spg_handle_t h, const int* in, int* out, int64_t n) {
     return scan_impl<int, int>(h, in, out, n);

@@ -246,6 +246,7 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
     C->priv = cp;
     if (algo == SPG_ALGO_AUTO) algo = rowwise_choose(h, A, B);
     cp->algo = algo;
+    h->stats.algo_used = (int32_t)algo;
     SPG_TRY(spg_alloc_t(h, &cp->plain.counters, 4));
     SPG_CUDA(h, cudaMemsetAsync(cp->plain.counters, 0, 4 * sizeof(unsigned long long), h->stream));
     SPG_TRY(spg_alloc_t(h, &cp->row_pairs, (size_t)A->tilem + 1));
@@ -334,6 +335,7 @@ extern "C" spg_status spg_spgemm(spg_handle_t h, const spg_tiles* A, const spg_t
     keep.tensor_pairs = h->stats.tensor_pairs;
     keep.fp64_tiles = h->stats.fp64_tiles;
     keep.work_items += h->stats.work_items;
+    keep.products = keep.products ? keep.products : h->stats.products;
     h->stats = keep;
     return s;
 }

@@ -118,6 +118,9 @@ spg_status spg_scan_i64_to_i64(spg_handle_t h, const int64_t* in, int64_t* out, 
 spg_status spg_radix_sort_pairs(spg_handle_t h, uint32_t* keys, uint32_t* vals, int64_t n,
                                 int key_bits);
 
+// v[i] = i for i < n.
+spg_status spg_iota_u32(spg_handle_t h, uint32_t* v, int64_t n);
+
 // Read a device scalar (synchronises the stream).
 spg_status spg_read_i64(spg_handle_t h, const int64_t* d, int64_t* out);
 spg_status spg_read_i32(spg_handle_t h, const int* d, int* out);

@@ -133,6 +133,8 @@ typedef struct {
     int64_t work_items;         /* row-wise windows launched                   */
     int64_t tensor_pairs;       /* tile pairs computed on tensor cores         */
     int64_t fp64_tiles;         /* C tiles recomputed in FP64                  */
+    int32_t algo_used;          /* spg_algo the symbolic phase ran             */
+    int32_t reserved;
 } spg_stats;
 
 /* ---- handle ---------------------------------------------------------------
@@ -211,6 +213,30 @@ spg_status spg_tiles_to_host(spg_handle_t h, const spg_tiles* T, int* tile_ptr, 
 
 /* Replaces the free calls at src/spgemm_raw_v2.cu:361-367. */
 spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C);
+
+/* ---- format conversions and chained products ------------------------------
+ * Device CSR transpose (m x n -> n x m), stable: rows stay ascending inside
+ * each column.  Replaces the host transpose of the --aat path
+ * (src/spgemm_raw_v2.cu:79-90).  Output arrays are caller-allocated device
+ * memory: out_rp n+1, out_ci / out_val nnz. */
+spg_status spg_csr_transpose(spg_handle_t h, int m, int n, int64_t nnz, const int* d_rp, const int* d_ci,
+                             const void* d_val, spg_dtype dtype, int* out_rp, int* out_ci, void* out_val);
+
+/* C's tiles -> device CSR (rows ascending, columns ascending), the device form
+   of the expansion at src/spgemm_raw_v2.cu:268-284.  Call with out_rp == NULL
+   to get *nnz only; then with caller-allocated device arrays (m+1, nnz, nnz). */
+spg_status spg_ctiles_to_csr(spg_handle_t h, const spg_ctiles* C, int* out_rp, int* out_ci, void* out_val,
+                             int64_t* nnz);
+
+/* Galerkin triple product RAP = P^T (A P) on the device (no reference
+   counterpart; it chains two of the reference's SpGEMMs): A (m x m) and P
+   (m x nc) are device CSR; A*P is formed, converted to CSR and re-tiled as the
+   B operand, P^T comes from spg_csr_transpose.  *products_out receives the
+   intermediate products of both SpGEMMs. */
+spg_status spg_galerkin(spg_handle_t h, int m, int nc, int64_t nnzA, const int* A_rp, const int* A_ci,
+                        const void* A_val, int64_t nnzP, const int* P_rp, const int* P_ci, const void* P_val,
+                        spg_dtype dtype, spg_algo algo, spg_precision prec, spg_ctiles* RAP,
+                        int64_t* products_out);
 
 /* Intermediate products sum_{(i,k) in A} nnz(B(k,:)) (src/spgemm_raw_v2.cu:95-99),
    computed on the device from the row views. */
