@@ -69,6 +69,18 @@ SIGNATURES = {
     "spg_products": (I32, [P, C.POINTER(SpgTiles), C.POINTER(SpgTiles), C.POINTER(I64)]),
     "spg_csr_transpose": (I32, [P, I32, I32, I64, P, P, P, I32, P, P, P]),
     "spg_ctiles_to_csr": (I32, [P, C.POINTER(SpgCTiles), P, P, P, C.POINTER(I64)]),
+    "spg_batch_create_host": (I32, [P, I32, P, P, P, P, P, P, P, P, P, P, P, I32, C.POINTER(P)]),
+    "spg_batch_free": (I32, [P, P]),
+    "spg_batch_spgemm": (I32, [P, P, I32, I32]),
+    "spg_batch_info": (I32, [P, P, I32, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)]),
+    "spg_batch_to_host": (I32, [P, P, I32, P, P, P, P, P, P, P, P]),
+    "spg_batch_set_values_host": (I32, [P, P, P, P]),
+    "spg_batch_numeric": (I32, [P, P, I32]),
+    "spg_batch_graph_capture": (I32, [P, P, P, P, P, I32]),
+    "spg_batch_graph_launch": (I32, [P, P]),
+    "spg_batch_bin_count": (I32, [P, P, C.POINTER(I32), P]),
+    "spg_batch_tune": (I32, [P, P, I32, C.POINTER(I32), P, P]),
+    "spg_batch_set_bins": (I32, [P, P, I32, P, P]),
     "spg_galerkin": (I32, [P, I32, I32, I64, P, P, P, I64, P, P, P, I32, I32, I32, C.POINTER(SpgCTiles),
                            C.POINTER(I64)]),
 }

@@ -295,3 +295,129 @@ def galerkin_device(handle: Handle, m, nc, nnza, a_rp, a_ci, a_val, nnzp, p_rp, 
                                          nnzp, C.c_void_p(p_rp), C.c_void_p(p_ci), C.c_void_p(p_val),
                                          _dtype_code(dtype), _ALGOS[algo], _PRECS[prec], C.byref(c), C.byref(prod)))
     return CTileMatrix(handle, c), prod.value
+
+
+class Batch:
+    """Many independent products C_p = A_p * B_p, one launch per phase per bin
+    (block-diagonal assembly on the device).  ``pairs`` is a list of (A, B)
+    host CSRs with A.n == B.m."""
+
+    def __init__(self, handle: Handle, pairs):
+        self.handle = handle
+        self.pairs = pairs
+        n = len(pairs)
+        dt = np.dtype(pairs[0][0].val.dtype)
+        self.dtype = dt
+        self._keep = []
+
+        def arr(xs, ct):
+            a = (ct * n)(*xs)
+            self._keep.append(a)
+            return a
+
+        def hold(x, dtype):
+            x = np.ascontiguousarray(x, dtype)
+            self._keep.append(x)
+            return x.ctypes.data
+
+        m = arr([a.m for a, b in pairs], C.c_int)
+        k = arr([a.n for a, b in pairs], C.c_int)
+        nn = arr([b.n for a, b in pairs], C.c_int)
+        na = arr([a.nnz for a, b in pairs], C.c_int64)
+        nb = arr([b.nnz for a, b in pairs], C.c_int64)
+        arp = arr([hold(a.row_ptr, np.int32) for a, b in pairs], C.c_void_p)
+        aci = arr([hold(a.col_idx, np.int32) for a, b in pairs], C.c_void_p)
+        av = arr([hold(a.val, dt) for a, b in pairs], C.c_void_p)
+        brp = arr([hold(b.row_ptr, np.int32) for a, b in pairs], C.c_void_p)
+        bci = arr([hold(b.col_idx, np.int32) for a, b in pairs], C.c_void_p)
+        bv = arr([hold(b.val, dt) for a, b in pairs], C.c_void_p)
+        self.b = C.c_void_p()
+        handle.check(handle.lib.spg_batch_create_host(handle.h, n, m, k, nn, na, arp, aci, av, nb, brp, bci, bv,
+                                                      _dtype_code(dt), C.byref(self.b)))
+
+    def spgemm(self, algo: str = "auto", prec: str = "f32"):
+        self.handle.check(self.handle.lib.spg_batch_spgemm(self.handle.h, self.b, _ALGOS[algo], _PRECS[prec]))
+
+    def numeric(self, prec: str = "f32"):
+        self.handle.check(self.handle.lib.spg_batch_numeric(self.handle.h, self.b, _PRECS[prec]))
+
+    def products(self) -> int:
+        p = C.c_int64()
+        self.handle.check(self.handle.lib.spg_batch_info(self.handle.h, self.b, -1, None, None, C.byref(p)))
+        return p.value
+
+    def tune(self, prec: str = "f32"):
+        nt = C.c_int()
+        thr = (C.c_int * 4)()
+        alg = (C.c_int * 4)()
+        self.handle.check(self.handle.lib.spg_batch_tune(self.handle.h, self.b, _PRECS[prec], C.byref(nt), thr, alg))
+        return list(thr[:nt.value]), list(alg[:nt.value + 1])
+
+    def set_bins(self, thresholds, algos=None):
+        t = (C.c_int * max(1, len(thresholds)))(*thresholds)
+        a = (C.c_int * (len(thresholds) + 1))(*[_ALGOS[x] if isinstance(x, str) else x for x in algos]) \
+            if algos else None
+        self.handle.check(self.handle.lib.spg_batch_set_bins(self.handle.h, self.b, len(thresholds), t, a))
+
+    def set_values(self, a_vals=None, b_vals=None):
+        n = len(self.pairs)
+        keep = []
+
+        def arr(vs):
+            if vs is None:
+                return None
+            xs = [np.ascontiguousarray(v, self.dtype) for v in vs]
+            keep.extend(xs)
+            return (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+        self.handle.check(self.handle.lib.spg_batch_set_values_host(self.handle.h, self.b, arr(a_vals), arr(b_vals)))
+
+    def result(self, p: int, values: bool = True) -> dict:
+        nt, nz = C.c_int64(), C.c_int64()
+        self.handle.check(self.handle.lib.spg_batch_info(self.handle.h, self.b, p, C.byref(nt), C.byref(nz), None))
+        a, b = self.pairs[p]
+        tilem = (a.m + TS - 1) // TS
+        out = dict(numtileC=nt.value, nnzC=nz.value, tile_ptrC=np.zeros(tilem + 1, np.int32),
+                   tile_rowidxC=np.zeros(nt.value, np.int32), tile_colidxC=np.zeros(nt.value, np.int32),
+                   maskC=np.zeros(nt.value * TS, np.uint16), tile_nnzC=np.zeros(nt.value + 1, np.int64),
+                   ptrRowC=np.zeros(nt.value * TS, np.uint8))
+        if values:
+            out.update(tile_valC=np.zeros(nz.value, self.dtype), tile_colC=np.zeros(nz.value, np.uint8))
+        g = out.get
+        self.handle.check(self.handle.lib.spg_batch_to_host(
+            self.handle.h, self.b, p, _ptr(out["tile_ptrC"]), _ptr(out["tile_rowidxC"]), _ptr(out["tile_colidxC"]),
+            _ptr(out["maskC"]), _ptr(out["tile_nnzC"]), _ptr(out["ptrRowC"]), _ptr(g("tile_valC")),
+            _ptr(g("tile_colC"))))
+        return out
+
+    def bins(self):
+        nb = C.c_int()
+        self.handle.check(self.handle.lib.spg_batch_bin_count(self.handle.h, self.b, C.byref(nb), None))
+        nz = (C.c_int64 * nb.value)()
+        self.handle.check(self.handle.lib.spg_batch_bin_count(self.handle.h, self.b, C.byref(nb), nz))
+        return list(nz)
+
+    def graph_capture(self, a_vals, b_vals, host_outs, prec: str = "f32"):
+        """host_outs: one pinned numpy buffer per bin (C values, block order)."""
+        n = len(self.pairs)
+        self._gkeep = [np.ascontiguousarray(v, self.dtype) for v in a_vals] + \
+                      [np.ascontiguousarray(v, self.dtype) for v in b_vals]
+        av = (C.c_void_p * n)(*[x.ctypes.data for x in self._gkeep[:n]])
+        bv = (C.c_void_p * n)(*[x.ctypes.data for x in self._gkeep[n:]])
+        ho = (C.c_void_p * len(host_outs))(*[x.ctypes.data if x is not None else None for x in host_outs])
+        self._gkeep += [av, bv, ho]
+        self.handle.check(self.handle.lib.spg_batch_graph_capture(self.handle.h, self.b, av, bv, ho, _PRECS[prec]))
+
+    def graph_launch(self):
+        self.handle.check(self.handle.lib.spg_batch_graph_launch(self.handle.h, self.b))
+
+    def free(self):
+        if self.b:
+            self.handle.lib.spg_batch_free(self.handle.h, self.b)
+            self.b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            if self.handle.h:
+                self.free()
+        except Exception:
+            pass

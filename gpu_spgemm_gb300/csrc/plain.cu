@@ -13,23 +13,44 @@ constexpr int C1_THREADS = 256;
 constexpr int C1_WARPS = C1_THREADS / 32;
 constexpr int SPEC_MAX = 32;  // pairs cached per C tile (MAX_MATCHED)
 
-// Union of B's tile columns over A's tiles (i,k) as a bitmap over tilenB.
-// Returns the number of tile pairs visited (valid in every thread's lane 0
-// partial; summed by the caller).
-__device__ int64_t build_c_bitmap(int i, int nwords, const int* __restrict__ a_tp,
-                                  const int* __restrict__ a_tc, const int* __restrict__ b_tp,
-                                  const int* __restrict__ b_tc, uint32_t* bm) {
+// Union of B's tile columns over A's tiles (i,k) as a bitmap.  The bitmap
+// covers only the tile-row's column span [jlo, jhi] (first / last tile column
+// of the B tile-rows it reaches; B's tile-rows are sorted), so clearing and
+// scanning cost O(span / 32) rather than O(tilenB / 32): a block-diagonal
+// batch of many small products stays cheap.  Word w of the bitmap holds
+// columns 32*(wlo + w) ... ; *s_span receives {wlo, nwd}.  Returns the tile
+// pairs visited (lane 0 partials).
+__device__ int64_t build_c_bitmap(int i, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
+                                  const int* __restrict__ b_tp, const int* __restrict__ b_tc, uint32_t* bm,
+                                  int* s_span) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int w = threadIdx.x; w < nwords; w += C1_THREADS) bm[w] = 0u;
-    __syncthreads();
-    int64_t pairs = 0;
     const int as = a_tp[i], ae = a_tp[i + 1];
+    if (threadIdx.x == 0) { s_span[0] = 0x7fffffff; s_span[1] = -1; }
+    __syncthreads();
+    int lo = 0x7fffffff, hi = -1;
+    for (int a = as + threadIdx.x; a < ae; a += C1_THREADS) {
+        const int k = __ldg(&a_tc[a]);
+        const int bs = __ldg(&b_tp[k]), be = __ldg(&b_tp[k + 1]);
+        if (be > bs) {
+            lo = min(lo, __ldg(&b_tc[bs]));
+            hi = max(hi, __ldg(&b_tc[be - 1]));
+        }
+    }
+    if (hi >= 0) { atomicMin(&s_span[0], lo); atomicMax(&s_span[1], hi); }
+    __syncthreads();
+    const int jlo = s_span[0], jhi = s_span[1];
+    const int wlo = jhi >= 0 ? (jlo >> 5) : 0;
+    const int nwd = jhi >= 0 ? (jhi >> 5) - wlo + 1 : 0;
+    for (int w = threadIdx.x; w < nwd; w += C1_THREADS) bm[w] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) { s_span[2] = wlo; s_span[3] = nwd; }
+    int64_t pairs = 0;
     for (int a = as + warp; a < ae; a += C1_WARPS) {
         const int k = __ldg(&a_tc[a]);
         const int bs = __ldg(&b_tp[k]), be = __ldg(&b_tp[k + 1]);
         pairs += be - bs;
         for (int b = bs + lane; b < be; b += 32) {
-            const int j = __ldg(&b_tc[b]);
+            const int j = __ldg(&b_tc[b]) - (wlo << 5);
             const uint32_t bit = 1u << (j & 31);
             if (!(bm[j >> 5] & bit)) atomicOr(&bm[j >> 5], bit);
         }
@@ -45,14 +66,17 @@ c1_count_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict_
     extern __shared__ uint32_t bm[];
     __shared__ int s_c[C1_WARPS];
     __shared__ int64_t s_p[C1_WARPS];
+    __shared__ int s_span[4];
     const int i = blockIdx.x;
+    (void)nwords;
     if (a_tp[i] == a_tp[i + 1]) {
         if (threadIdx.x == 0) { cnt[i] = 0; row_pairs[i] = 0; }
         return;
     }
-    int64_t pairs = build_c_bitmap(i, nwords, a_tp, a_tc, b_tp, b_tc, bm);
+    int64_t pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
+    const int nwd = s_span[3];
     int c = 0;
-    for (int w = threadIdx.x; w < nwords; w += C1_THREADS) c += __popc(bm[w]);
+    for (int w = threadIdx.x; w < nwd; w += C1_THREADS) c += __popc(bm[w]);
     c = warp_sum(c);
     pairs = warp_sum(pairs);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -74,11 +98,14 @@ c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__
                const int* __restrict__ tile_ptrC, int* __restrict__ rowidxC, int* __restrict__ colidxC) {
     extern __shared__ uint32_t bm[];
     __shared__ int64_t s_sh[C1_WARPS + 1];
+    __shared__ int s_span[4];
     const int i = blockIdx.x;
+    (void)nwords;
     if (tile_ptrC[i] == tile_ptrC[i + 1]) return;
-    build_c_bitmap(i, nwords, a_tp, a_tc, b_tp, b_tc, bm);
-    const int wpt = (nwords + C1_THREADS - 1) / C1_THREADS;
-    const int w0 = min(nwords, (int)threadIdx.x * wpt), w1 = min(nwords, w0 + wpt);
+    build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
+    const int wlo = s_span[2], nwd = s_span[3];
+    const int wpt = (nwd + C1_THREADS - 1) / C1_THREADS;
+    const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
     int64_t local = 0;
     for (int w = w0; w < w1; w++) local += __popc(bm[w]);
     int64_t tot;
@@ -89,7 +116,7 @@ c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__
         while (bits) {
             const int b = __ffs(bits) - 1;
             rowidxC[pos] = i;
-            colidxC[pos] = w * 32 + b;
+            colidxC[pos] = (wlo + w) * 32 + b;
             pos++;
             bits &= bits - 1u;
         }

@@ -23,6 +23,10 @@ struct CPriv {
     RowwisePriv rw;
 };
 
+RowwisePriv* ctiles_rowwise_priv(spg_ctiles* C) {
+    return C && C->priv ? &static_cast<CPriv*>(C->priv)->rw : nullptr;
+}
+
 // ---------------------------------------------------------------------------
 // handle and helpers
 // ---------------------------------------------------------------------------

@@ -41,7 +41,22 @@ tiler_count_kernel(int m, int n, int nwords, const int* __restrict__ rp, const i
         if (threadIdx.x == 0) tile_cnt[i] = 0;
         return;
     }
-    for (int w = threadIdx.x; w < nwords; w += TL_THREADS) bm[w] = 0u;
+    __shared__ int s_span[2];
+    if (threadIdx.x == 0) { s_span[0] = 0x7fffffff; s_span[1] = -1; }
+    __syncthreads();
+    if (threadIdx.x < (unsigned)(r1 - r0)) {
+        const int s = rp[r0 + threadIdx.x], e = rp[r0 + threadIdx.x + 1];
+        if (e > s) {
+            atomicMin(&s_span[0], min(max(ci[s], 0), n - 1) >> 4);
+            atomicMax(&s_span[1], min(max(ci[e - 1], 0), n - 1) >> 4);
+        }
+    }
+    __syncthreads();
+    const int wlo = s_span[1] >= 0 ? (s_span[0] >> 5) : 0;
+    // non-canonical rows can put columns outside [first, last]; those set the
+    // error flag and are skipped, so a span from the row ends is safe
+    const int nwd_span = s_span[1] >= 0 ? (s_span[1] >> 5) - wlo + 1 : 0;
+    for (int w = threadIdx.x; w < nwd_span; w += TL_THREADS) bm[w] = 0u;
     __syncthreads();
     for (int r = r0 + warp; r < r1; r += TL_WARPS) {
         const int s = rp[r], e = rp[r + 1];
@@ -54,12 +69,14 @@ tiler_count_kernel(int m, int n, int nwords, const int* __restrict__ rp, const i
             }
             const int tc = c >> 4;
             if (j > s && (prev >> 4) == tc) continue;  // segment already marked
-            atomicOr(&bm[tc >> 5], 1u << (tc & 31));
+            const int w = (tc >> 5) - wlo;
+            if (w < 0 || w >= nwd_span) { atomicOr(flags, DERR_NONCANONICAL); continue; }
+            atomicOr(&bm[w], 1u << (tc & 31));
         }
     }
     __syncthreads();
     int cnt = 0;
-    for (int w = threadIdx.x; w < nwords; w += TL_THREADS) cnt += __popc(bm[w]);
+    for (int w = threadIdx.x; w < nwd_span; w += TL_THREADS) cnt += __popc(bm[w]);
     cnt = warp_sum(cnt);
     if (lane == 0) s_red[warp] = cnt;
     __syncthreads();
@@ -70,27 +87,37 @@ tiler_count_kernel(int m, int n, int nwords, const int* __restrict__ rp, const i
     }
 }
 
-// Builds the tile-column bitmap of tile-row i and its per-word exclusive
-// popcount prefix in shared memory (bm[0..nwords), pre[0..nwords)).
-__device__ void build_rank_table(int i, int m, int nwords, const int* __restrict__ rp,
-                                 const int* __restrict__ ci, uint32_t* bm, uint32_t* pre,
-                                 int64_t* s_sh) {
+// Builds the tile-column bitmap of tile-row i over its column span (first /
+// last column of its rows; the CSR was validated canonical by the count pass)
+// and the per-word exclusive popcount prefix: bm[0..nwd), pre[0..nwd) hold
+// words wlo .. wlo+nwd-1.  Returns {wlo, nwd} in s_span.
+__device__ void build_rank_table(int i, int m, const int* __restrict__ rp, const int* __restrict__ ci,
+                                 uint32_t* bm, uint32_t* pre, int64_t* s_sh, int* s_span) {
     const int r0 = i * TS, r1 = min(r0 + TS, m);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int w = threadIdx.x; w < nwords; w += TL_THREADS) bm[w] = 0u;
+    if (threadIdx.x == 0) { s_span[0] = 0x7fffffff; s_span[1] = -1; }
+    __syncthreads();
+    if (threadIdx.x < (unsigned)(r1 - r0)) {
+        const int s = rp[r0 + threadIdx.x], e = rp[r0 + threadIdx.x + 1];
+        if (e > s) { atomicMin(&s_span[0], ci[s] >> 4); atomicMax(&s_span[1], ci[e - 1] >> 4); }
+    }
+    __syncthreads();
+    const int wlo = s_span[1] >= 0 ? (s_span[0] >> 5) : 0;
+    const int nwd = s_span[1] >= 0 ? (s_span[1] >> 5) - wlo + 1 : 0;
+    for (int w = threadIdx.x; w < nwd; w += TL_THREADS) bm[w] = 0u;
     __syncthreads();
     for (int r = r0 + warp; r < r1; r += TL_WARPS) {
         const int s = rp[r], e = rp[r + 1];
         for (int j = s + lane; j < e; j += 32) {
             const int tc = ci[j] >> 4;
             if (j > s && (ci[j - 1] >> 4) == tc) continue;
-            atomicOr(&bm[tc >> 5], 1u << (tc & 31));
+            atomicOr(&bm[(tc >> 5) - wlo], 1u << (tc & 31));
         }
     }
     __syncthreads();
     // blocked word ranges per thread
-    const int wpt = (nwords + TL_THREADS - 1) / TL_THREADS;
-    const int w0 = min(nwords, (int)threadIdx.x * wpt), w1 = min(nwords, w0 + wpt);
+    const int wpt = (nwd + TL_THREADS - 1) / TL_THREADS;
+    const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
     int64_t local = 0;
     for (int w = w0; w < w1; w++) local += __popc(bm[w]);
     int64_t tot;
@@ -99,11 +126,12 @@ __device__ void build_rank_table(int i, int m, int nwords, const int* __restrict
         pre[w] = (uint32_t)run;
         run += __popc(bm[w]);
     }
+    if (threadIdx.x == 0) { s_span[2] = wlo; s_span[3] = nwd; }
     __syncthreads();
 }
 
-__device__ __forceinline__ int rank_of(const uint32_t* bm, const uint32_t* pre, int tc) {
-    const int w = tc >> 5;
+__device__ __forceinline__ int rank_of(const uint32_t* bm, const uint32_t* pre, int wlo, int tc) {
+    const int w = (tc >> 5) - wlo;
     return (int)pre[w] + __popc(bm[w] & ((1u << (tc & 31)) - 1u));
 }
 
@@ -116,22 +144,24 @@ tiler_fill_kernel(int m, int nwords, const int* __restrict__ rp, const int* __re
     uint32_t* bm = sm;
     uint32_t* pre = sm + nwords;
     __shared__ int64_t s_sh[TL_WARPS + 1];
+    __shared__ int s_span[4];
     const int i = blockIdx.x;
     const int r0 = i * TS, r1 = min(r0 + TS, m);
     if (rp[r0] == rp[r1]) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    build_rank_table(i, m, nwords, rp, ci, bm, pre, s_sh);
+    build_rank_table(i, m, rp, ci, bm, pre, s_sh, s_span);
+    const int wlo = s_span[2], nwd = s_span[3];
     const int tbase = tile_ptr[i];
     // sorted tile columns of this tile-row
     {
-        const int wpt = (nwords + TL_THREADS - 1) / TL_THREADS;
-        const int w0 = min(nwords, (int)threadIdx.x * wpt), w1 = min(nwords, w0 + wpt);
+        const int wpt = (nwd + TL_THREADS - 1) / TL_THREADS;
+        const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
         for (int w = w0; w < w1; w++) {
             uint32_t bits = bm[w];
             int pos = tbase + (int)pre[w];
             while (bits) {
                 const int b = __ffs(bits) - 1;
-                tile_columnidx[pos] = w * 32 + b;
+                tile_columnidx[pos] = (wlo + w) * 32 + b;
                 if (tile_rowof) tile_rowof[pos] = i;
                 pos++;
                 bits &= bits - 1u;
@@ -143,7 +173,7 @@ tiler_fill_kernel(int m, int nwords, const int* __restrict__ rp, const int* __re
         const int s = rp[r], e = rp[r + 1], rl = r - r0;
         for (int j = s + lane; j < e; j += 32) {
             const int c = ci[j], tc = c >> 4;
-            const int t = tbase + rank_of(bm, pre, tc);
+            const int t = tbase + rank_of(bm, pre, wlo, tc);
             int p = 0;
             for (int q = j - 1; q >= s && (ci[q] >> 4) == tc; q--) p++;
             tmp_t[j] = t;

@@ -197,13 +197,20 @@ def stencil27_dof3(g: int = 64, dof: int = 3, seed: int = SEED, dtype=np.float32
 # Erdos-Renyi batch
 # ----------------------------------------------------------------------------
 def erdos_renyi(n: int, avg_deg: float, rng: np.random.Generator, dtype=np.float32) -> CSR:
-    """G(n, p) with p = avg_deg / n: the edge count is Binomial(n^2, p), edges are
-    drawn uniformly and duplicates merged.  Values U[-1, 1]."""
-    p = avg_deg / n
-    e = int(rng.binomial(n * n, p))
-    r = rng.integers(0, n, size=e, dtype=np.int64)
-    c = rng.integers(0, n, size=e, dtype=np.int64)
-    r, c = _merge_keys(n, n, r, c)
+    """G(n, p) with p = avg_deg / n: every (i, j) present independently with
+    probability p.  Drawn as a Bernoulli process over the row-major index
+    i*n + j (geometric gaps, cumulative sum), so entries come out sorted and
+    unique with no sort.  Values U[-1, 1]."""
+    p = min(1.0, avg_deg / n)
+    total = n * n
+    est = int(total * p + 8 * np.sqrt(total * p) + 64)
+    gaps = rng.geometric(p, size=est).astype(np.int64)
+    lin = np.cumsum(gaps) - 1
+    while lin[-1] < total - 1 and lin.size:  # rare: extend the process
+        more = rng.geometric(p, size=max(64, est // 8)).astype(np.int64)
+        lin = np.concatenate([lin, lin[-1] + np.cumsum(more)])
+    lin = lin[lin < total]
+    r, c = lin // n, lin % n
     vals = (rng.random(r.size) * 2.0 - 1.0).astype(dtype)
     return _from_coo_sorted_unique(n, n, r, c, vals)
 

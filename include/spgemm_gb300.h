@@ -238,6 +238,51 @@ spg_status spg_galerkin(spg_handle_t h, int m, int nc, int64_t nnzA, const int* 
                         spg_dtype dtype, spg_algo algo, spg_precision prec, spg_ctiles* RAP,
                         int64_t* products_out);
 
+/* ---- batches of independent products -----------------------------------
+ * No reference counterpart: the reference multiplies one matrix per run
+ * (src/spgemm_raw_v2.cu:61).  A batch C_p = A_p * B_p (p < nprob, A_p m_p x
+ * k_p, B_p k_p x n_p, host CSR) is assembled on the device as block-diagonal
+ * products (one per bin of problems, blocks at 16-aligned offsets) and each
+ * phase runs as one launch for the whole bin. */
+typedef struct spg_batch_s* spg_batch_t;
+
+spg_status spg_batch_create_host(spg_handle_t h, int nprob, const int* m, const int* k, const int* n,
+                                 const int64_t* nnzA, const int* const* A_rp, const int* const* A_ci,
+                                 const void* const* A_val, const int64_t* nnzB, const int* const* B_rp,
+                                 const int* const* B_ci, const void* const* B_val, spg_dtype dtype,
+                                 spg_batch_t* out);
+spg_status spg_batch_free(spg_handle_t h, spg_batch_t b);
+/* Steps 1-3 for every problem (AUTO: each bin's tuned algorithm). */
+spg_status spg_batch_spgemm(spg_handle_t h, spg_batch_t b, spg_algo algo, spg_precision prec);
+/* Problem p's C sizes (p < 0: only *products, the batch's total). */
+spg_status spg_batch_info(spg_handle_t h, spg_batch_t b, int p, int64_t* numtileC, int64_t* nnzC,
+                          int64_t* products);
+/* Problem p's C arrays with problem-local indices (layout of spg_ctiles). */
+spg_status spg_batch_to_host(spg_handle_t h, spg_batch_t b, int p, int* tile_ptrC, int* tile_rowidxC,
+                             int* tile_colidxC, uint16_t* maskC, int64_t* tile_nnzC, uint8_t* ptrRowC,
+                             void* tile_valC, uint8_t* tile_colC);
+/* New values (same structure) from host arrays; NULL entries are kept. */
+spg_status spg_batch_set_values_host(spg_handle_t h, spg_batch_t b, const void* const* A_val,
+                                     const void* const* B_val);
+/* Numeric phase only, one launch per bin, no host synchronisation. */
+spg_status spg_batch_numeric(spg_handle_t h, spg_batch_t b, spg_precision prec);
+/* Capture, per bin, [values host->device, numeric, C values -> host_vals_out[bin]]
+   into a CUDA graph (the handle must use a non-default stream); replay with
+   spg_batch_graph_launch.  Host buffers should be pinned. */
+spg_status spg_batch_graph_capture(spg_handle_t h, spg_batch_t b, const void* const* A_val,
+                                   const void* const* B_val, void* const* host_vals_out, spg_precision prec);
+spg_status spg_batch_graph_launch(spg_handle_t h, spg_batch_t b);
+/* Number of bins and each bin's C nonzeros (for sizing host_vals_out). */
+spg_status spg_batch_bin_count(spg_handle_t h, spg_batch_t b, int* nbins, int64_t* nnz_per_bin);
+/* Autotuner: tries bin thresholds on n (none, median, terciles) and, per bin,
+   the plain and row-wise algorithms, timing each on the batch; keeps the
+   fastest.  thresholds_out gets <= 2 values, algos_out <= 3. */
+spg_status spg_batch_tune(spg_handle_t h, spg_batch_t b, spg_precision prec, int* n_thresholds,
+                          int* thresholds_out, int* algos_out);
+/* Set bins explicitly: n_thresholds ascending upper bounds on n, algos per bin. */
+spg_status spg_batch_set_bins(spg_handle_t h, spg_batch_t b, int n_thresholds, const int* thresholds,
+                              const int* algos);
+
 /* Intermediate products sum_{(i,k) in A} nnz(B(k,:)) (src/spgemm_raw_v2.cu:95-99),
    computed on the device from the row views. */
 spg_status spg_products(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int64_t* out);

@@ -156,11 +156,14 @@ def numeric(TA: dict, TB: dict, S: dict) -> dict:
     l = lib()
     valC = np.zeros(S["nnzC"], np.float64)
     colC = np.zeros(S["nnzC"], np.uint8)
+    # converted copies are bound to names so they outlive the C call
+    a_val = np.ascontiguousarray(TA["tile_csr_Val"], np.float64)
+    b_val = np.ascontiguousarray(TB["tile_csr_Val"], np.float64)
     l.orc_step3_numeric(S["numtileC"], _p(S["tile_rowidxC"]), _p(S["tile_colidxC"]),
                         _p(TA["tile_ptr"]), _p(TA["tile_columnidx"]), _p(TA["tile_nnz"]),
-                        _p(np.ascontiguousarray(TA["tile_csr_Val"], np.float64)), _p(TA["tile_csr_Col"]),
+                        _p(a_val), _p(TA["tile_csr_Col"]),
                         _p(TA["tile_csr_Ptr"]), _p(TB["csc_tile_ptr"]), _p(TB["csc_tile_rowidx"]),
-                        _p(TB["tile_nnz"]), _p(np.ascontiguousarray(TB["tile_csr_Val"], np.float64)),
+                        _p(TB["tile_nnz"]), _p(b_val),
                         _p(TB["tile_csr_Col"]), _p(TB["tile_csr_Ptr"]), _p(S["tile_nnzC"]),
                         _p(S["maskC"]), _p(S["ptrRowC"]), _p(valC), _p(colC))
     return dict(tile_valC=valC, tile_colC=colC)
@@ -178,15 +181,19 @@ def spgemm_tiles(a, b) -> dict:
 def tiles_to_csr(m: int, n: int, S: dict):
     """Expand C tiles to CSR (src/spgemm_raw_v2.cu:268-284)."""
     l = lib()
+    # converted copies are bound to names so they outlive the C calls
+    rowidx = np.ascontiguousarray(S["tile_rowidxC"], np.int32)
+    colidx = np.ascontiguousarray(S["tile_colidxC"], np.int32)
+    nnzc = np.ascontiguousarray(S["tile_nnzC"], np.int64)
+    colc = np.ascontiguousarray(S["tile_colC"], np.uint8)
+    valc = np.ascontiguousarray(S["tile_valC"], np.float64)
     rp = np.zeros(m + 1, np.int64)
-    l.orc_tiles_to_csr(m, n, S["numtileC"], _p(S["tile_rowidxC"]), _p(S["tile_colidxC"]),
-                       _p(np.ascontiguousarray(S["tile_nnzC"], np.int64)), _p(S["tile_colC"]),
-                       _p(np.ascontiguousarray(S["tile_valC"], np.float64)), _p(rp), None, None)
+    l.orc_tiles_to_csr(m, n, int(S["numtileC"]), _p(rowidx), _p(colidx), _p(nnzc), _p(colc), _p(valc), _p(rp),
+                       None, None)
     cols = np.zeros(int(rp[-1]), np.int32)
     vals = np.zeros(int(rp[-1]), np.float64)
-    l.orc_tiles_to_csr(m, n, S["numtileC"], _p(S["tile_rowidxC"]), _p(S["tile_colidxC"]),
-                       _p(np.ascontiguousarray(S["tile_nnzC"], np.int64)), _p(S["tile_colC"]),
-                       _p(np.ascontiguousarray(S["tile_valC"], np.float64)), _p(rp), _p(cols), _p(vals))
+    l.orc_tiles_to_csr(m, n, int(S["numtileC"]), _p(rowidx), _p(colidx), _p(nnzc), _p(colc), _p(valc), _p(rp),
+                       _p(cols), _p(vals))
     return rp, cols, vals
 
 
