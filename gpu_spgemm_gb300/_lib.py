@@ -45,7 +45,7 @@ class SpgCTiles(C.Structure):
 class SpgStats(C.Structure):
     _fields_ = [("ms_step1", C.c_float), ("ms_step2", C.c_float), ("ms_step3", C.c_float),
                 ("products", I64), ("overflow_reruns", I64), ("work_items", I64), ("tensor_pairs", I64),
-                ("fp64_tiles", I64), ("algo_used", I32), ("reserved", I32)]
+                ("fp64_tiles", I64), ("algo_used", I32), ("reserved", I32), ("predicted_tiles", I64)]
 
 
 # name -> (restype, argtypes); every symbol the header declares
@@ -81,6 +81,17 @@ SIGNATURES = {
     "spg_batch_bin_count": (I32, [P, P, C.POINTER(I32), P]),
     "spg_batch_tune": (I32, [P, P, I32, C.POINTER(I32), P, P]),
     "spg_batch_set_bins": (I32, [P, P, I32, P, P]),
+    "spg_mlp_num_params": (I32, []),
+    "spg_mlp_num_features": (I32, []),
+    "spg_mlp_create": (I32, [P, P, P, C.POINTER(P)]),
+    "spg_mlp_free": (I32, [P, P]),
+    "spg_mlp_get_params": (I32, [P, P, P, P]),
+    "spg_mlp_set_norm": (I32, [P, P, P]),
+    "spg_mlp_features": (I32, [P, C.POINTER(SpgTiles), C.POINTER(SpgTiles), P]),
+    "spg_mlp_forward": (I32, [P, P, P, I64, P]),
+    "spg_mlp_gradient": (I32, [P, P, P, P, I64, P, P]),
+    "spg_mlp_train": (I32, [P, P, P, P, I64, P, I32, I32, C.c_float, P]),
+    "spg_set_sizing_model": (I32, [P, P, C.c_float]),
     "spg_galerkin": (I32, [P, I32, I32, I64, P, P, P, I64, P, P, P, I32, I32, I32, C.POINTER(SpgCTiles),
                            C.POINTER(I64)]),
 }

@@ -421,3 +421,100 @@ class Batch:
                 self.free()
         except Exception:
             pass
+
+
+import os as _os
+
+SIZING_MODEL_PATH = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "sizing_mlp.npz")
+
+
+class SizingModel:
+    """Learned sizing of C (8 -> 32 -> 32 -> 2 MLP on per-tile-row features),
+    trained and evaluated by the library's own CUDA kernels."""
+
+    NF, NO, NNORM = 8, 2, 20
+
+    def __init__(self, handle: Handle, params=None, norm=None):
+        self.handle = handle
+        self.nparam = handle.lib.spg_mlp_num_params()
+        self.m = C.c_void_p()
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        n = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        handle.check(handle.lib.spg_mlp_create(handle.h, _ptr(p), _ptr(n), C.byref(self.m)))
+
+    @classmethod
+    def load(cls, handle: Handle, path: str = SIZING_MODEL_PATH):
+        z = np.load(path)
+        return cls(handle, z["params"], z["norm"])
+
+    def params(self):
+        p = np.zeros(self.nparam, np.float32)
+        n = np.zeros(self.NNORM, np.float32)
+        self.handle.check(self.handle.lib.spg_mlp_get_params(self.handle.h, self.m, _ptr(p), _ptr(n)))
+        return p, n
+
+    def set_norm(self, norm):
+        n = np.ascontiguousarray(norm, np.float32)
+        self.handle.check(self.handle.lib.spg_mlp_set_norm(self.handle.h, self.m, _ptr(n)))
+
+    def features(self, A: TileMatrix, B: TileMatrix):
+        import torch
+        f = torch.zeros((max(A.tilem, 1), self.NF), dtype=torch.float32, device="cuda")
+        self.handle.check(self.handle.lib.spg_mlp_features(self.handle.h, C.byref(A.t), C.byref(B.t),
+                                                           C.c_void_p(f.data_ptr())))
+        return f[:A.tilem]
+
+    def predict(self, feat):
+        import torch
+        out = torch.zeros((max(feat.shape[0], 1), self.NO), dtype=torch.float32, device="cuda")
+        self.handle.check(self.handle.lib.spg_mlp_forward(self.handle.h, self.m, C.c_void_p(feat.data_ptr()),
+                                                          feat.shape[0], C.c_void_p(out.data_ptr())))
+        return out[:feat.shape[0]]
+
+    def gradient(self, feat, target):
+        import torch
+        g = torch.zeros(self.nparam, dtype=torch.float32, device="cuda")
+        loss = C.c_float()
+        self.handle.check(self.handle.lib.spg_mlp_gradient(self.handle.h, self.m, C.c_void_p(feat.data_ptr()),
+                                                           C.c_void_p(target.data_ptr()), feat.shape[0],
+                                                           C.c_void_p(g.data_ptr()), C.byref(loss)))
+        return g.cpu().numpy(), loss.value
+
+    def train(self, feat, target, epochs=20, batch=8192, lr=3e-3, seed=0):
+        import torch
+        n = feat.shape[0]
+        gen = torch.Generator(device="cpu").manual_seed(seed)
+        perm = torch.cat([torch.randperm(n, generator=gen) for _ in range(epochs)]).to(torch.int32).cuda()
+        loss = C.c_float()
+        self.handle.check(self.handle.lib.spg_mlp_train(self.handle.h, self.m, C.c_void_p(feat.data_ptr()),
+                                                        C.c_void_p(target.data_ptr()), n,
+                                                        C.c_void_p(perm.data_ptr()), epochs, batch, lr,
+                                                        C.byref(loss)))
+        return loss.value
+
+    def attach(self, margin: float = 0.25):
+        self.handle.check(self.handle.lib.spg_set_sizing_model(self.handle.h, self.m, margin))
+
+    def detach(self):
+        self.handle.check(self.handle.lib.spg_set_sizing_model(self.handle.h, None, 0.0))
+
+    def save(self, path: str, **meta):
+        p, n = self.params()
+        np.savez(path, params=p, norm=n, **meta)
+
+    def free(self):
+        if self.m:
+            self.handle.lib.spg_mlp_free(self.handle.h, self.m)
+            self.m = C.c_void_p()
+
+
+def sizing_targets(Cm: CTileMatrix):
+    """Per C tile-row: log1p(C tiles), log1p(C nonzeros) as a (tilem, 2) float32
+    device tensor (from the exact symbolic phase)."""
+    import torch
+    h = Cm.to_host(values=False)
+    tp = h["tile_ptrC"].astype(np.int64)
+    ntc = np.diff(tp)
+    nz = h["tile_nnzC"][tp[1:]] - h["tile_nnzC"][tp[:-1]]
+    t = np.stack([np.log1p(ntc), np.log1p(nz)], axis=1).astype(np.float32)
+    return torch.from_numpy(t).cuda()

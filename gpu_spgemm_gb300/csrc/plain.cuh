@@ -15,6 +15,10 @@ struct PlainPriv {
 
 spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                        int64_t* row_pairs, unsigned long long* pairs_total);
+spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                             int64_t* row_pairs, unsigned long long* pairs_total, int64_t cap);
+spg_status mlp_predict_capacity(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int64_t* cap_tiles,
+                                int64_t* cap_nnz);
 spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                        PlainPriv* pp, int* tile_cnt);
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,

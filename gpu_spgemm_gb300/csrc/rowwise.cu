@@ -35,7 +35,7 @@ constexpr int NW_MAXT = 1024;   // C tiles per numeric window
 constexpr int NW_VALS = 8192;   // C values per numeric window
 constexpr int MAXA_SMEM = 1024; // A nonzeros per tile-row whose cursors fit in shared memory
 constexpr int SHORT = 8;        // B entries a lane handles alone before handing a segment to a warp
-constexpr int LONG_CAP = 512;   // segments queued for warp-cooperative processing per pass
+constexpr int LONG_CAP = 1024;  // segments queued for warp-cooperative processing per window
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
     while (lo < hi) {
@@ -203,58 +203,64 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const
                                             const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                                             const int* __restrict__ b_ci, int2* s_long, int* s_nlong, Op op) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    while (true) {
-        if (tid == 0) *s_nlong = 0;
-        __syncthreads();
-        int pending = 0;
-        for (int x = tid; x < it.na; x += RW_THREADS) {
-            const int2 cs = cur[x];
-            if (cs.y >= limit) continue;
-            const int e = it.e0 + x;
-            const int k = __ldg(&a_ci[e]);
-            const int be = __ldg(&b_rp[k + 1]);
-            const int r = row_of(s_rows, e);
-            int p = cs.x, c = cs.y, cnt = 0;
-            while (c < limit && cnt < SHORT) {
-                op(x, r, p, c);
-                p++;
-                cnt++;
-                c = p < be ? __ldg(&b_ci[p]) : INT_MAX;
-            }
-            if (c < limit) {
-                const int slot = atomicAdd(s_nlong, 1);
-                if (slot < LONG_CAP) s_long[slot] = make_int2(x, p);
-                else pending = 1;
-            }
-            cur[x] = make_int2(p, c);
+    if (tid == 0) *s_nlong = 0;
+    __syncthreads();
+    for (int x = tid; x < it.na; x += RW_THREADS) {
+        const int2 cs = cur[x];
+        if (cs.y >= limit) continue;
+        const int e = it.e0 + x;
+        const int k = __ldg(&a_ci[e]);
+        const int be = __ldg(&b_rp[k + 1]);
+        const int r = row_of(s_rows, e);
+        int p = cs.x, c = cs.y, cnt = 0;
+        while (c < limit && cnt < SHORT) {
+            op(x, r, p, c);
+            p++;
+            cnt++;
+            c = p < be ? __ldg(&b_ci[p]) : INT_MAX;
         }
-        __syncthreads();
-        const int nl = min(*s_nlong, LONG_CAP);
-        for (int y = warp; y < nl; y += RW_WARPS) {
-            const int x = s_long[y].x;
-            const int e = it.e0 + x;
-            const int k = __ldg(&a_ci[e]);
-            const int be = __ldg(&b_rp[k + 1]);
-            const int r = row_of(s_rows, e);
-            int p = s_long[y].y, nextc = INT_MAX;
-            while (true) {
-                const int q = p + lane;
-                const int c = q < be ? __ldg(&b_ci[q]) : INT_MAX;
-                const bool in = c < limit;
-                const unsigned bal = __ballot_sync(0xffffffffu, in);
-                if (in) op(x, r, q, c);
-                const int n_in = __popc(bal);
-                if (n_in < 32) {
-                    nextc = __shfl_sync(0xffffffffu, c, n_in);
-                    p += n_in;
-                    break;
+        if (c < limit) {
+            const int slot = atomicAdd(s_nlong, 1);
+            if (slot < LONG_CAP) {
+                s_long[slot] = make_int2(x, p);
+            } else {
+                // queue full: finish the segment here (never a second pass over
+                // all nonzeros of the tile-row)
+                while (c < limit) {
+                    op(x, r, p, c);
+                    p++;
+                    c = p < be ? __ldg(&b_ci[p]) : INT_MAX;
                 }
-                p += 32;
             }
-            if (lane == 0) cur[x] = make_int2(p, nextc);
         }
-        if (!__syncthreads_or(pending)) break;
+        cur[x] = make_int2(p, c);
     }
+    __syncthreads();
+    const int nl = min(*s_nlong, LONG_CAP);
+    for (int y = warp; y < nl; y += RW_WARPS) {
+        const int x = s_long[y].x;
+        const int e = it.e0 + x;
+        const int k = __ldg(&a_ci[e]);
+        const int be = __ldg(&b_rp[k + 1]);
+        const int r = row_of(s_rows, e);
+        int p = s_long[y].y, nextc = INT_MAX;
+        while (true) {
+            const int q = p + lane;
+            const int c = q < be ? __ldg(&b_ci[q]) : INT_MAX;
+            const bool in = c < limit;
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            if (in) op(x, r, q, c);
+            const int n_in = __popc(bal);
+            if (n_in < 32) {
+                nextc = __shfl_sync(0xffffffffu, c, n_in);
+                p += n_in;
+                break;
+            }
+            p += 32;
+        }
+        if (lane == 0) cur[x] = make_int2(p, nextc);
+    }
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------

@@ -256,7 +256,14 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
     SPG_TRY(spg_alloc_t(h, &cp->row_pairs, (size_t)A->tilem + 1));
     SPG_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
     // ---- step 1: C tile structure
-    SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
+    if (h->sizing) {
+        int64_t cap_t = 0, cap_z = 0;
+        SPG_TRY(mlp_predict_capacity(h, A, B, &cap_t, &cap_z));
+        h->stats.predicted_tiles = cap_t;
+        SPG_TRY(plain_step1_sized(h, A, B, C, cp->row_pairs, cp->plain.counters + 2, cap_t));
+    } else {
+        SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
+    }
     SPG_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
     const int64_t nt = C->numtileC;
     // ---- step 2: bitmask symbolic

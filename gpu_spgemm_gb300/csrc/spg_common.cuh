@@ -72,6 +72,8 @@ __device__ __forceinline__ T block_excl_scan(T v, T* sh, T* total) {
 // ---------------------------------------------------------------------------
 struct spg_handle_s {
     int device = 0;
+    struct spg_mlp_s* sizing = nullptr;  // learned sizing model (optional)
+    float sizing_margin = 0.25f;
     cudaStream_t stream = nullptr;
     std::string err;
     spg_stats stats{};

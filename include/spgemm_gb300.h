@@ -135,6 +135,7 @@ typedef struct {
     int64_t fp64_tiles;         /* C tiles recomputed in FP64                  */
     int32_t algo_used;          /* spg_algo the symbolic phase ran             */
     int32_t reserved;
+    int64_t predicted_tiles;    /* C tile capacity from the sizing model (0: none) */
 } spg_stats;
 
 /* ---- handle ---------------------------------------------------------------
@@ -282,6 +283,38 @@ spg_status spg_batch_tune(spg_handle_t h, spg_batch_t b, spg_precision prec, int
 /* Set bins explicitly: n_thresholds ascending upper bounds on n, algos per bin. */
 spg_status spg_batch_set_bins(spg_handle_t h, spg_batch_t b, int n_thresholds, const int* thresholds,
                               const int* algos);
+
+/* ---- learned sizing --------------------------------------------------------
+ * No reference counterpart: the reference sizes C by a full counting pass and
+ * a host read-back before filling (src/spgemm_raw_v2.cu:119-156).  An MLP
+ * (8 per-tile-row features -> 32 -> 32 -> 2) predicts each C tile-row's tile
+ * count and nonzeros; with a model attached (spg_set_sizing_model) step 1
+ * pre-sizes C from the predicted total and runs as one fused pass, the exact
+ * count inside it judging the prediction (too small => exact re-run of the
+ * fill; stats.overflow_reruns).  The model is trained on the GPU by
+ * spg_mlp_train (forward, backward and Adam kernels of this library). */
+typedef struct spg_mlp_s* spg_mlp_t;
+int spg_mlp_num_params(void);
+int spg_mlp_num_features(void);
+/* host_params (spg_mlp_num_params floats) / host_norm (20 floats: feature
+   mean[8], feature inv-std[8], target mean[2], target std[2]) may be NULL. */
+spg_status spg_mlp_create(spg_handle_t h, const float* host_params, const float* host_norm, spg_mlp_t* out);
+spg_status spg_mlp_free(spg_handle_t h, spg_mlp_t m);
+spg_status spg_mlp_get_params(spg_handle_t h, spg_mlp_t m, float* host_params, float* host_norm);
+spg_status spg_mlp_set_norm(spg_handle_t h, spg_mlp_t m, const float* host_norm);
+/* Features of C = A*B per tile-row of A into d_feat (A->tilem x 8 floats). */
+spg_status spg_mlp_features(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, float* d_feat);
+/* Predictions (log1p of C tiles and C nonzeros per tile-row), n x 2 floats. */
+spg_status spg_mlp_forward(spg_handle_t h, spg_mlp_t m, const float* d_feat, int64_t n, float* d_out);
+/* Gradient of the mean squared error (standardised targets) without update. */
+spg_status spg_mlp_gradient(spg_handle_t h, spg_mlp_t m, const float* d_feat, const float* d_target, int64_t n,
+                            float* d_grad_out, float* loss_out);
+/* Adam, `epochs` passes, mini-batches of `batch`; d_perm: epochs*n sample
+   indices (NULL = in order). */
+spg_status spg_mlp_train(spg_handle_t h, spg_mlp_t m, const float* d_feat, const float* d_target, int64_t n,
+                         const int* d_perm, int epochs, int batch, float lr, float* last_epoch_loss);
+/* Attach (m) or detach (NULL) the sizing model; capacity = prediction * (1+margin). */
+spg_status spg_set_sizing_model(spg_handle_t h, spg_mlp_t m, float margin);
 
 /* Intermediate products sum_{(i,k) in A} nnz(B(k,:)) (src/spgemm_raw_v2.cu:95-99),
    computed on the device from the row views. */

@@ -1,0 +1,86 @@
+"""Learned sizing: CUDA MLP gradients against the numpy restatement; training
+lowers the loss; with the trained model attached step 1 runs as one fused
+pass with the exact same C structure; a model that under-predicts triggers
+the exact re-run and still gives the exact structure."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp_ref
+from gpu_spgemm_gb300 import api, synth
+
+pytestmark = pytest.mark.gpu
+KEYS = ["tile_ptrC", "tile_rowidxC", "tile_colidxC", "maskC", "tile_nnzC", "ptrRowC", "tile_colC"]
+
+
+def test_gradient_matches_numpy(handle):
+    rng = np.random.default_rng(0)
+    params = (rng.standard_normal(mlp_ref.NPARAM) * 0.2).astype(np.float32)
+    norm = np.concatenate([rng.standard_normal(8) * 0.1, 1 + rng.random(8), rng.standard_normal(2),
+                           1 + rng.random(2)]).astype(np.float32)
+    X = rng.standard_normal((777, 8)).astype(np.float32)
+    Y = rng.standard_normal((777, 2)).astype(np.float32)
+    m = api.SizingModel(handle, params, norm)
+    g, loss = m.gradient(torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda())
+    gr, lr = mlp_ref.gradient(params, norm, X, Y)
+    assert abs(loss - lr) <= 1e-4 * max(1.0, lr)
+    assert np.linalg.norm(g - gr) <= 1e-4 * np.linalg.norm(gr)
+    out = m.predict(torch.from_numpy(X).cuda()).cpu().numpy()
+    _, _, _, o = mlp_ref.forward(params, norm, X)
+    np.testing.assert_allclose(out, o * norm[18:20] + norm[16:18], rtol=1e-4, atol=1e-4)
+    m.free()
+
+
+def test_training_lowers_loss(handle):
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((20000, 8)).astype(np.float32)
+    Y = np.stack([np.sin(X[:, 0]) + X[:, 1], X[:, 2] * X[:, 3]], 1).astype(np.float32)
+    Xt, Yt = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
+    m = api.SizingModel(handle)
+    _, l0 = m.gradient(Xt, Yt)
+    l1 = m.train(Xt, Yt, epochs=15, batch=1024, lr=3e-3)
+    assert l1 < 0.5 * l0, (l0, l1)
+    m.free()
+
+
+def _run(handle, a, model=None, margin=0.25):
+    if model is not None:
+        model.attach(margin)
+    try:
+        A = api.csr2tile(handle, a)
+        B = api.build_csc_tiles(handle, a)
+        C = api.spgemm(handle, A, B)
+        st = handle.stats()
+        return C.to_host(), st
+    finally:
+        if model is not None:
+            model.detach()
+
+
+@pytest.mark.skipif(not os.path.exists(api.SIZING_MODEL_PATH), reason="no trained sizing model shipped")
+@pytest.mark.parametrize("name,a", [("rmat_15", synth.rmat(15, 16)), ("stencil27_12", synth.stencil27_dof3(12)),
+                                    ("poisson2d_128", synth.poisson2d(128, np.float32))])
+def test_trained_sizing_single_pass_same_structure(handle, name, a):
+    model = api.SizingModel.load(handle)
+    ref, st0 = _run(handle, a)
+    got, st1 = _run(handle, a, model)
+    for k in KEYS:
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    assert st0["predicted_tiles"] == 0
+    assert st1["predicted_tiles"] >= got["numtileC"]   # the trained model sized C: one fused pass
+    assert st1["overflow_reruns"] == 0
+    model.free()
+
+
+def test_underprediction_reruns_exactly(handle):
+    params = np.zeros(mlp_ref.NPARAM, np.float32)  # predicts log1p(count) = 0 everywhere
+    m = api.SizingModel(handle, params)
+    a = synth.rmat(13, 16)
+    ref, _ = _run(handle, a)
+    got, st = _run(handle, a, m, margin=0.0)
+    for k in KEYS:
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    assert st["overflow_reruns"] >= 1
+    m.free()
