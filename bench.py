@@ -270,6 +270,8 @@ def run_ours(args):
     total_bytes = a_b + b_b + c_b
     hbm_steps = total_bytes / (ms * 1e-3) / 1e9
 
+    accuracy = value_check(h, api, a, b, args) if args.check else None
+
     # ---- end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
@@ -290,7 +292,9 @@ def run_ours(args):
                     "l2": "inputs and outputs exceed L2 (A,B tiles %.2f GB, C %.1f GB > 129 MB)" %
                           ((a_b + b_b) / 1e9, c_b / 1e9),
                     "ms_step1": s1, "ms_step2": s2, "ms_step3": s3,
-                    "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak})
+                    "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak,
+                    "tensor_pairs": stats[-1].get("tensor_pairs", 0), "fp64_tiles": stats[-1].get("fp64_tiles", 0),
+                    "accuracy": accuracy})
         line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": np.dtype(dtype).name, "data": "synthetic",
@@ -300,6 +304,37 @@ def run_ours(args):
     h.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def value_check(h, api, a, b, args, tile_rows=512):
+    """Relative Frobenius error of C's values against the FP64 oracle on the
+    first `tile_rows` C tile-rows (each C tile-row depends only on the same
+    16 rows of A, so the oracle multiplies that row block of A by B)."""
+    import ctypes as C
+    import oracle
+    from gpu_spgemm_gb300 import _lib as L
+    rows = min(a.m, 16 * tile_rows)
+    asub = synth.CSR(rows, a.n, a.row_ptr[:rows + 1].copy(), a.col_idx[:a.row_ptr[rows]].copy(),
+                     a.val[:a.row_ptr[rows]].copy())
+    S = oracle.spgemm_tiles(asub, b)
+    A = api.csr2tile(h, a)
+    B = api.build_csc_tiles(h, b)
+    Cm = api.spgemm(h, A, B, algo=args.algo, prec=args.prec)
+    nt = int(S["numtileC"])
+    nv = int(S["nnzC"])
+    vd = np.float64 if a.val.dtype == np.float64 else np.float32
+    vals = np.zeros(max(nv, 1), vd)
+    cols = np.zeros(max(nv, 1), np.uint8)
+    got = C.c_int64()
+    h.check(h.lib.spg_ctiles_to_host_range(h.h, C.byref(Cm.c), 0, nt, None, None, None, None, None,
+                                           vals.ctypes.data, cols.ctypes.data, max(nv, 1), C.byref(got)))
+    st = h.stats()
+    Cm.free(); A.free(); B.free()
+    ref = S["tile_valC"]
+    err = float(np.linalg.norm(vals[:nv].astype(np.float64) - ref) / (np.linalg.norm(ref) or 1.0))
+    return {"tile_rows_checked": int(rows // 16), "c_values_checked": nv, "rel_frob_vs_fp64": err,
+            "cols_equal": bool(np.array_equal(cols[:nv], S["tile_colC"])), "tensor_pairs": st["tensor_pairs"],
+            "fp64_tiles": st["fp64_tiles"]}
 
 
 def gpu_launches(algo):
@@ -472,6 +507,7 @@ def main():
     p.add_argument("--cpu-s", type=float, default=12.0)
     p.add_argument("--ref-step-s", type=float, default=8.0)
     p.add_argument("--batch-count", type=int, default=512)
+    p.add_argument("--check", action="store_true", help="value error vs the FP64 oracle on a prefix of C")
     p.add_argument("--traffic", type=float, default=None,
                    help="dram bytes per launch of the dominant kernel from an ncu capture")
     args = p.parse_args()

@@ -4,6 +4,8 @@
 // structure, one half-warp per C tile for the symbolic phase, one warp per C
 // tile with register accumulators for the numeric phase.  This is the baseline
 // the row-wise binned path is measured against.
+#include <cuda_fp16.h>
+
 #include "spg_common.cuh"
 #include "plain.cuh"
 
@@ -415,6 +417,261 @@ c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision (SPG_PREC_MIXED, FP32 data): the per-C-tile kernel above,
+// with every matched tile pair whose A and B tiles both hold >= dense_thr
+// nonzeros computed as a real 16x16x16 contraction on the tensor cores:
+// mma.sync m16n8k16, FP16 operands, FP32 accumulation, each FP32 value split
+// x = hi + lo (hi = fp16(x), lo = fp16(x - hi)) and hi*hi + hi*lo + lo*hi
+// accumulated (the dropped lo*lo term is ~2^-22 relative).  tcgen05.mma needs
+// M >= 64; one 16x16 tile pair fills a single m16n8k16 pair exactly, and
+// stacking tile pairs to M = 64/128 would multiply mostly zero padding on
+// these sparse tile rows.  Each lane builds its fragments straight from the
+// compressed tile (16-bit row masks + popc offsets): no shared-memory
+// densification.  A |A|*|B| magnitude product (hi parts) flags C tiles whose
+// entries cancelled to below cancel_eps of their magnitude; those tiles are
+// recomputed in FP64 by c3_fp64_list_kernel.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// element (r, c) of a compressed tile: value if present, else 0
+__device__ __forceinline__ float tile_elem(const float* __restrict__ vals, int base, uint32_t mask_r, int ptr_r,
+                                           int c) {
+    if (!((mask_r >> (15 - c)) & 1u)) return 0.f;
+    return __ldg(&vals[base + ptr_r + __popc(mask_r >> (16 - c))]);
+}
+
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_t& lo, uint32_t& ab) {
+    const __half h0 = __float2half_rn(x0), h1 = __float2half_rn(x1);
+    const __half l0 = __float2half_rn(x0 - __half2float(h0)), l1 = __float2half_rn(x1 - __half2float(h1));
+    const __half2 H = __halves2half2(h0, h1), Lo = __halves2half2(l0, l1);
+    hi = *reinterpret_cast<const uint32_t*>(&H);
+    lo = *reinterpret_cast<const uint32_t*>(&Lo);
+    const __half2 A = __habs2(H);
+    ab = *reinterpret_cast<const uint32_t*>(&A);
+}
+
+template <bool CACHE>
+__global__ void __launch_bounds__(256)
+c3_mixed_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
+                const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ a_tnnz,
+                const float* __restrict__ a_val, const uint8_t* __restrict__ a_col, const uint8_t* __restrict__ a_ptr16,
+                const uint16_t* __restrict__ a_mask, const int* __restrict__ b_cscp, const int* __restrict__ b_cscr,
+                const int* __restrict__ b_tnnz, const float* __restrict__ b_val, const uint8_t* __restrict__ b_ptr16,
+                const uint16_t* __restrict__ b_mask, const int64_t* __restrict__ tile_nnzC,
+                const uint16_t* __restrict__ maskC, const uint8_t* __restrict__ ptrRowC, float* __restrict__ valC,
+                uint8_t* __restrict__ colC, const int* __restrict__ spec_cnt, const int* __restrict__ spec_off,
+                const int* __restrict__ spec_pa, const int* __restrict__ spec_pb, int dense_thr, float cancel_eps,
+                unsigned long long* __restrict__ tensor_pairs, int* __restrict__ flag_list,
+                unsigned* __restrict__ nflag) {
+    __shared__ float s_tile[8][TS][TS + 1];
+    __shared__ float s_mag[8][TS][TS + 1];
+    const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
+    const int g = lane >> 2, tq = lane & 3;
+    const int wib = threadIdx.x >> 5;
+    unsigned long long my_tensor = 0;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib; t < numtileC; t += nwarps) {
+        const int64_t cbase = tile_nnzC[t];
+        if (tile_nnzC[t + 1] == cbase) continue;
+        float acc[TS];
+#pragma unroll
+        for (int c = 0; c < TS; c++) acc[c] = 0.f;
+        float d[8], mg[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) { d[q] = 0.f; mg[q] = 0.f; }
+        auto do_pair = [&](int pa, int pb) {
+            const int sA = __ldg(&a_tnnz[pa]), na = __ldg(&a_tnnz[pa + 1]) - sA;
+            const int sB = __ldg(&b_tnnz[pb]), nb = __ldg(&b_tnnz[pb + 1]) - sB;
+            if (na >= dense_thr && nb >= dense_thr) {  // warp-uniform: tensor-core pair
+                __syncwarp();  // mma.sync.aligned: the whole warp converged
+                if (lane == 0) my_tensor++;
+                uint32_t ah[4], al[4], aa[4];
+                {
+                    const uint32_t m0 = __ldg(&a_mask[(int64_t)pa * TS + g]);
+                    const uint32_t m1 = __ldg(&a_mask[(int64_t)pa * TS + g + 8]);
+                    const int p0 = __ldg(&a_ptr16[(int64_t)pa * TS + g]);
+                    const int p1 = __ldg(&a_ptr16[(int64_t)pa * TS + g + 8]);
+                    const int c0 = 2 * tq;
+                    split2(tile_elem(a_val, sA, m0, p0, c0), tile_elem(a_val, sA, m0, p0, c0 + 1), ah[0], al[0], aa[0]);
+                    split2(tile_elem(a_val, sA, m1, p1, c0), tile_elem(a_val, sA, m1, p1, c0 + 1), ah[1], al[1], aa[1]);
+                    split2(tile_elem(a_val, sA, m0, p0, c0 + 8), tile_elem(a_val, sA, m0, p0, c0 + 9), ah[2], al[2],
+                           aa[2]);
+                    split2(tile_elem(a_val, sA, m1, p1, c0 + 8), tile_elem(a_val, sA, m1, p1, c0 + 9), ah[3], al[3],
+                           aa[3]);
+                }
+                const int k0 = 2 * tq;
+                const uint32_t bm0 = __ldg(&b_mask[(int64_t)pb * TS + k0]);
+                const uint32_t bm1 = __ldg(&b_mask[(int64_t)pb * TS + k0 + 1]);
+                const uint32_t bm2 = __ldg(&b_mask[(int64_t)pb * TS + k0 + 8]);
+                const uint32_t bm3 = __ldg(&b_mask[(int64_t)pb * TS + k0 + 9]);
+                const int bp0 = __ldg(&b_ptr16[(int64_t)pb * TS + k0]);
+                const int bp1 = __ldg(&b_ptr16[(int64_t)pb * TS + k0 + 1]);
+                const int bp2 = __ldg(&b_ptr16[(int64_t)pb * TS + k0 + 8]);
+                const int bp3 = __ldg(&b_ptr16[(int64_t)pb * TS + k0 + 9]);
+#pragma unroll
+                for (int nh = 0; nh < 2; nh++) {
+                    const int n = g + 8 * nh;
+                    uint32_t bh[2], bl[2], ba[2];
+                    split2(tile_elem(b_val, sB, bm0, bp0, n), tile_elem(b_val, sB, bm1, bp1, n), bh[0], bl[0], ba[0]);
+                    split2(tile_elem(b_val, sB, bm2, bp2, n), tile_elem(b_val, sB, bm3, bp3, n), bh[1], bl[1], ba[1]);
+                    mma16816(d + 4 * nh, ah, bh);
+                    mma16816(d + 4 * nh, ah, bl);
+                    mma16816(d + 4 * nh, al, bh);
+                    mma16816(mg + 4 * nh, aa, ba);
+                }
+                return;
+            }
+            const int rs = __ldg(&a_ptr16[(int64_t)pa * TS + r]);
+            const int re = (r == TS - 1) ? na : (int)__ldg(&a_ptr16[(int64_t)pa * TS + r + 1]);
+            for (int e = rs + hsel; e < re; e += 2) {
+                const int kk = __ldg(&a_col[sA + e]) & 15;
+                const float va = __ldg(&a_val[sA + e]);
+                const uint32_t mb = __ldg(&b_mask[(int64_t)pb * TS + kk]);
+                int off = sB + __ldg(&b_ptr16[(int64_t)pb * TS + kk]);
+#pragma unroll
+                for (int c = 0; c < TS; c++) {
+                    if (mb & (0x8000u >> c)) {
+                        acc[c] = fmaf(va, __ldg(&b_val[off]), acc[c]);
+                        off++;
+                    }
+                }
+            }
+        };
+        int cnt = CACHE ? spec_cnt[t] : -1;
+        if (cnt >= 0) {
+            const int off = spec_off[t];
+            for (int q = 0; q < cnt; q++) do_pair(spec_pa[off + q], spec_pb[off + q]);
+        } else {
+            const int bi = rowidxC[t], bj = colidxC[t];
+            const int as = a_tp[bi], ae = a_tp[bi + 1];
+            const int bs = b_cscp[bj], be = b_cscp[bj + 1];
+            const bool a_short = (ae - as) <= (be - bs);
+            const int ss = a_short ? as : bs, se = a_short ? ae : be;
+            const int ls = a_short ? bs : as, le = a_short ? be : ae;
+            const int* sl = a_short ? a_tc : b_cscr;
+            const int* ll = a_short ? b_cscr : a_tc;
+            for (int base = ss; base < se; base += 32) {
+                const int idx = base + lane;
+                int pos = -1;
+                if (idx < se) {
+                    const int key = __ldg(&sl[idx]);
+                    const int p = lower_bound_dev(ll, ls, le, key);
+                    if (p < le && __ldg(&ll[p]) == key) pos = p;
+                }
+                unsigned mm = __ballot_sync(0xffffffffu, pos >= 0);
+                while (mm) {
+                    const int src = __ffs(mm) - 1;
+                    mm &= mm - 1u;
+                    const int sp = __shfl_sync(0xffffffffu, idx, src);
+                    const int lp = __shfl_sync(0xffffffffu, pos, src);
+                    do_pair(a_short ? sp : lp, a_short ? lp : sp);
+                }
+            }
+        }
+        // combine tensor fragments and register accumulators in shared memory
+#pragma unroll
+        for (int nh = 0; nh < 2; nh++) {
+            const int c = 2 * tq + 8 * nh;
+            s_tile[wib][g][c] = d[4 * nh + 0];
+            s_tile[wib][g][c + 1] = d[4 * nh + 1];
+            s_tile[wib][g + 8][c] = d[4 * nh + 2];
+            s_tile[wib][g + 8][c + 1] = d[4 * nh + 3];
+            s_mag[wib][g][c] = mg[4 * nh + 0];
+            s_mag[wib][g][c + 1] = mg[4 * nh + 1];
+            s_mag[wib][g + 8][c] = mg[4 * nh + 2];
+            s_mag[wib][g + 8][c + 1] = mg[4 * nh + 3];
+        }
+#pragma unroll
+        for (int c = 0; c < TS; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+        __syncwarp();
+        int flagged = 0;
+        if (hsel == 0) {
+            const uint32_t mc = maskC[t * TS + r];
+            int64_t p = cbase + ptrRowC[t * TS + r];
+#pragma unroll
+            for (int c = 0; c < TS; c++) {
+                if (mc & (0x8000u >> c)) {
+                    const float v = acc[c] + s_tile[wib][r][c];
+                    const float mag = s_mag[wib][r][c];
+                    if (mag > 0.f && fabsf(v) < cancel_eps * mag) flagged = 1;
+                    valC[p] = v;
+                    colC[p] = (uint8_t)((r << 4) | c);
+                    p++;
+                }
+            }
+        }
+        if (__any_sync(0xffffffffu, flagged) && lane == 0) flag_list[atomicAdd(nflag, 1u)] = (int)t;
+        __syncwarp();
+    }
+    my_tensor = warp_sum(my_tensor);
+    if (lane == 0 && my_tensor) atomicAdd(tensor_pairs, my_tensor);
+}
+
+// FP64 recomputation of the flagged C tiles (warp per tile, FP32 data).
+__global__ void __launch_bounds__(256)
+c3_fp64_list_kernel(int nlist, const int* __restrict__ list, const int* __restrict__ rowidxC,
+                    const int* __restrict__ colidxC, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
+                    const int* __restrict__ a_tnnz, const float* __restrict__ a_val, const uint8_t* __restrict__ a_col,
+                    const uint8_t* __restrict__ a_ptr16, const int* __restrict__ b_cscp, const int* __restrict__ b_cscr,
+                    const int* __restrict__ b_tnnz, const float* __restrict__ b_val,
+                    const uint8_t* __restrict__ b_ptr16, const uint16_t* __restrict__ b_mask,
+                    const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
+                    const uint8_t* __restrict__ ptrRowC, float* __restrict__ valC) {
+    const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nlist; w += nw) {
+        const int64_t t = list[w];
+        double acc[TS];
+#pragma unroll
+        for (int c = 0; c < TS; c++) acc[c] = 0.0;
+        const int bi = rowidxC[t], bj = colidxC[t];
+        int a = a_tp[bi];
+        const int ae = a_tp[bi + 1];
+        int b = b_cscp[bj];
+        const int be = b_cscp[bj + 1];
+        while (a < ae && b < be) {  // merge of the two sorted tile lists, warp-uniform
+            const int ka = __ldg(&a_tc[a]), kb = __ldg(&b_cscr[b]);
+            if (ka < kb) { a++; continue; }
+            if (kb < ka) { b++; continue; }
+            const int sA = __ldg(&a_tnnz[a]), na = __ldg(&a_tnnz[a + 1]) - sA;
+            const int rs = __ldg(&a_ptr16[(int64_t)a * TS + r]);
+            const int re = (r == TS - 1) ? na : (int)__ldg(&a_ptr16[(int64_t)a * TS + r + 1]);
+            const int sB = __ldg(&b_tnnz[b]);
+            for (int e = rs + hsel; e < re; e += 2) {
+                const int kk = __ldg(&a_col[sA + e]) & 15;
+                const double va = __ldg(&a_val[sA + e]);
+                const uint32_t mb = __ldg(&b_mask[(int64_t)b * TS + kk]);
+                int off = sB + __ldg(&b_ptr16[(int64_t)b * TS + kk]);
+#pragma unroll
+                for (int c = 0; c < TS; c++) {
+                    if (mb & (0x8000u >> c)) {
+                        acc[c] = fma(va, (double)__ldg(&b_val[off]), acc[c]);
+                        off++;
+                    }
+                }
+            }
+            a++;
+            b++;
+        }
+#pragma unroll
+        for (int c = 0; c < TS; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+        if (hsel == 0) {
+            const uint32_t mc = maskC[t * TS + r];
+            int64_t p = tile_nnzC[t] + ptrRowC[t * TS + r];
+#pragma unroll
+            for (int c = 0; c < TS; c++)
+                if (mc & (0x8000u >> c)) valC[p++] = (float)acc[c];
+        }
+    }
+}
+
 __global__ void i64_to_i32_kernel(const int64_t* __restrict__ in, int* __restrict__ out, int64_t n) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
         out[t] = (int)in[t];
@@ -595,4 +852,54 @@ static spg_status plain_step3_t(spg_handle_t h, const spg_tiles* A, const spg_ti
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp) {
     if (A->dtype == SPG_F64) return plain_step3_t<double>(h, A, B, C, pp);
     return plain_step3_t<float>(h, A, B, C, pp);
+}
+
+// Mixed-precision numeric (FP32 data): dense tile pairs on tensor cores, the
+// rest on FP32 registers, cancellation-flagged C tiles recomputed in FP64.
+spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
+                             int dense_thr, float cancel_eps) {
+    const int64_t nt = C->numtileC;
+    if (nt == 0 || C->nnzC == 0) return SPG_OK;
+    if (A->dtype != SPG_F32) return spg_fail(h, SPG_ERR_INVALID, "mixed precision needs FP32 data");
+    unsigned long long* ctr = nullptr;
+    int* list = nullptr;
+    SPG_TRY(spg_alloc_t(h, &ctr, 2));
+    SPG_TRY(spg_alloc_t(h, &list, (size_t)nt + 1));
+    SPG_CUDA(h, cudaMemsetAsync(ctr, 0, 16, h->stream));
+    const int grid = grid_cap(h, nt, 8, 32);
+    const bool cache = pp && pp->spec_cap > 0;
+#define MIXED_ARGS                                                                                                  \
+    nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const float*)A->tile_csr_Val, \
+        A->tile_csr_Col, A->tile_csr_Ptr, A->mask, B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz,               \
+        (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,                \
+        (float*)C->tile_valC, C->tile_colC
+    if (cache)
+        c3_mixed_kernel<true><<<grid, 256, 0, h->stream>>>(MIXED_ARGS, pp->spec_cnt, pp->spec_off, pp->spec_pa,
+                                                            pp->spec_pb, dense_thr, cancel_eps, ctr,
+                                                            list, reinterpret_cast<unsigned*>(ctr + 1));
+    else
+        c3_mixed_kernel<false><<<grid, 256, 0, h->stream>>>(MIXED_ARGS, nullptr, nullptr, nullptr, nullptr, dense_thr,
+                                                             cancel_eps, ctr, list,
+                                                             reinterpret_cast<unsigned*>(ctr + 1));
+#undef MIXED_ARGS
+    SPG_CUDA(h, cudaGetLastError());
+    int64_t v[2] = {0, 0};
+    SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 20, ctr, 16, cudaMemcpyDeviceToHost, h->stream));
+    SPG_CUDA(h, cudaStreamSynchronize(h->stream));
+    v[0] = h->h_pinned[20];
+    v[1] = (int64_t)(uint32_t)h->h_pinned[21];
+    h->stats.tensor_pairs = v[0];
+    h->stats.fp64_tiles = v[1];
+    if (v[1] > 0) {
+        const int g2 = grid_cap(h, v[1], 8, 32);
+        c3_fp64_list_kernel<<<g2, 256, 0, h->stream>>>(
+            (int)v[1], list, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            (const float*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
+            B->tile_nnz, (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC,
+            C->ptrRowC, (float*)C->tile_valC);
+        SPG_CUDA(h, cudaGetLastError());
+    }
+    spg_free_async(h, ctr);
+    spg_free_async(h, list);
+    return SPG_OK;
 }

@@ -23,6 +23,8 @@ spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
                        PlainPriv* pp, int* tile_cnt);
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                        PlainPriv* pp);
+spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
+                             int dense_thr, float cancel_eps);
 
 spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int* d_rp, const int* d_ci,
                            const void* d_val, spg_dtype dtype, spg_layout layout, int flags, spg_tiles* out);

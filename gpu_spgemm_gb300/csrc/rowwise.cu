@@ -34,8 +34,7 @@ constexpr int WS = 2048;        // C tiles per symbolic window
 constexpr int NW_MAXT = 1024;   // C tiles per numeric window
 constexpr int NW_VALS = 8192;   // C values per numeric window
 constexpr int MAXA_SMEM = 1024; // A nonzeros per tile-row whose cursors fit in shared memory
-constexpr int SHORT = 8;        // B entries a lane handles alone before handing a segment to a warp
-constexpr int LONG_CAP = 1024;  // segments queued for warp-cooperative processing per window
+constexpr int HEAVY = 64;       // B rows longer than this are walked by a whole warp
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
     while (lo < hi) {
@@ -194,71 +193,79 @@ __device__ __forceinline__ int row_of(const int* s_rows, int e) {
 
 // Runs `op(x, r, p, c)` for every B entry (position p, column c < limit) that
 // the A nonzeros of the tile-row reach inside the current window, advancing
-// each nonzero's cursor past the window.  One lane per A nonzero walks up to
-// SHORT entries of its B row alone (R-MAT: most (nonzero, window) visits hold
-// one or two products); longer segments are queued and finished by a whole
-// warp, 32 entries per step.  `op` is called with the A-nonzero index x.
+// each nonzero's cursor past the window.  Each warp takes 32 A nonzeros at a
+// time, one per lane.  A lane whose B row is short (<= HEAVY entries in all)
+// walks its few entries in this window alone; the lanes whose B row is long
+// (the hub rows of a power-law matrix) are then taken one at a time by the
+// whole warp, which reads 128 entries per round trip (four independent loads
+// per lane) so the walk is bound by throughput, not by load latency.  No
+// queue, no second pass.  `op` is called with the A-nonzero index x.
 template <typename Op>
 __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const int* s_rows, int limit,
                                             const int* __restrict__ a_ci, const int* __restrict__ b_rp,
-                                            const int* __restrict__ b_ci, int2* s_long, int* s_nlong, Op op) {
+                                            const int* __restrict__ b_ci, Op op) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) *s_nlong = 0;
-    __syncthreads();
-    for (int x = tid; x < it.na; x += RW_THREADS) {
-        const int2 cs = cur[x];
-        if (cs.y >= limit) continue;
-        const int e = it.e0 + x;
-        const int k = __ldg(&a_ci[e]);
-        const int be = __ldg(&b_rp[k + 1]);
-        const int r = row_of(s_rows, e);
-        int p = cs.x, c = cs.y, cnt = 0;
-        while (c < limit && cnt < SHORT) {
-            op(x, r, p, c);
-            p++;
-            cnt++;
-            c = p < be ? __ldg(&b_ci[p]) : INT_MAX;
+    for (int base = warp * 32; base < it.na; base += RW_THREADS) {
+        const int x = base + lane;
+        int2 cs = make_int2(0, INT_MAX);
+        int k = 0, bs = 0, be = 0;
+        if (x < it.na) {
+            cs = cur[x];
+            if (cs.y < limit) {
+                k = __ldg(&a_ci[it.e0 + x]);
+                bs = __ldg(&b_rp[k]);
+                be = __ldg(&b_rp[k + 1]);
+            }
         }
-        if (c < limit) {
-            const int slot = atomicAdd(s_nlong, 1);
-            if (slot < LONG_CAP) {
-                s_long[slot] = make_int2(x, p);
-            } else {
-                // queue full: finish the segment here (never a second pass over
-                // all nonzeros of the tile-row)
-                while (c < limit) {
-                    op(x, r, p, c);
-                    p++;
-                    c = p < be ? __ldg(&b_ci[p]) : INT_MAX;
+        const bool has = cs.y < limit;
+        const bool heavy = has && (be - bs) > HEAVY;
+        const int r = has ? row_of(s_rows, it.e0 + x) : 0;
+        if (has && !heavy) {
+            int p = cs.x, c = cs.y;
+            while (c < limit) {
+                const int cn = (p + 1 < be) ? __ldg(&b_ci[p + 1]) : INT_MAX;  // next column, loaded early
+                op(x, r, p, c);
+                p++;
+                c = cn;
+            }
+            cur[x] = make_int2(p, c);
+        }
+        unsigned hm = __ballot_sync(0xffffffffu, heavy);
+        while (hm) {
+            const int src = __ffs(hm) - 1;
+            hm &= hm - 1u;
+            const int hx = base + src;
+            const int hr = __shfl_sync(0xffffffffu, r, src);
+            const int hbe = __shfl_sync(0xffffffffu, be, src);
+            int p = __shfl_sync(0xffffffffu, cs.x, src), nextc = INT_MAX;
+            while (true) {
+                int cc[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int q = p + 32 * u + lane;
+                    cc[u] = q < hbe ? __ldg(&b_ci[q]) : INT_MAX;
                 }
+                int n = 0;
+                bool stop = false;
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const bool in = cc[u] < limit;
+                    if (in) op(hx, hr, p + 32 * u + lane, cc[u]);
+                    const unsigned bal = __ballot_sync(0xffffffffu, in);
+                    const int nu = __popc(bal);
+                    if (!stop && nu < 32) {
+                        nextc = __shfl_sync(0xffffffffu, cc[u], nu);
+                        n += nu;
+                        stop = true;
+                    } else if (!stop) {
+                        n += 32;
+                    }
+                }
+                p += n;
+                if (stop) break;
             }
+            if (lane == 0) cur[hx] = make_int2(p, nextc);
         }
-        cur[x] = make_int2(p, c);
-    }
-    __syncthreads();
-    const int nl = min(*s_nlong, LONG_CAP);
-    for (int y = warp; y < nl; y += RW_WARPS) {
-        const int x = s_long[y].x;
-        const int e = it.e0 + x;
-        const int k = __ldg(&a_ci[e]);
-        const int be = __ldg(&b_rp[k + 1]);
-        const int r = row_of(s_rows, e);
-        int p = s_long[y].y, nextc = INT_MAX;
-        while (true) {
-            const int q = p + lane;
-            const int c = q < be ? __ldg(&b_ci[q]) : INT_MAX;
-            const bool in = c < limit;
-            const unsigned bal = __ballot_sync(0xffffffffu, in);
-            if (in) op(x, r, q, c);
-            const int n_in = __popc(bal);
-            if (n_in < 32) {
-                nextc = __shfl_sync(0xffffffffu, c, n_in);
-                p += n_in;
-                break;
-            }
-            p += 32;
-        }
-        if (lane == 0) cur[x] = make_int2(p, nextc);
     }
     __syncthreads();
 }
@@ -280,8 +287,6 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
-    __shared__ int2 s_long[LONG_CAP];
-    __shared__ int s_nlong;
     const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
@@ -295,7 +300,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, s_long, &s_nlong,
+            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci,
                         [&](int, int r, int, int c) {
                             const int lt = wrank(bm, pre, wlo, c >> 4);
                             const int idx = r * WS + lt;
@@ -352,8 +357,6 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
     __shared__ int s_nt;
-    __shared__ int2 s_long[LONG_CAP];
-    __shared__ int s_nlong;
     const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
@@ -393,7 +396,7 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, s_long, &s_nlong,
+            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci,
                         [&](int x, int r, int p, int c) {
                             const int lt = wrank(bm, pre, wlo, c >> 4);
                             const uint32_t m16 = mk[lt * TS + r];

@@ -326,7 +326,10 @@ extern "C" spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_
     if (algo == SPG_ALGO_AUTO) algo = cp->algo;
     if (algo == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) algo = SPG_ALGO_PLAIN;
     SPG_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
-    if (algo == SPG_ALGO_ROWWISE || prec == SPG_PREC_MIXED || (prec == SPG_PREC_F64 && A->dtype == SPG_F32)) {
+    if (prec == SPG_PREC_MIXED && A->dtype == SPG_F32) {
+        // dense tile pairs on tensor cores (plain per-C-tile structure)
+        SPG_TRY(plain_step3_mixed(h, A, B, C, &cp->plain, h->dense_thr, h->cancel_eps));
+    } else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32)) {
         SPG_TRY(rowwise_numeric(h, A, B, C, &cp->rw, prec));
     } else {
         SPG_TRY(plain_step3(h, A, B, C, &cp->plain));

@@ -164,3 +164,14 @@ def test_matches_reference_kernels_fixture(handle, path, algo):
     for k in STRUCT_KEYS:
         np.testing.assert_array_equal(got[k], z[k].astype(got[k].dtype), err_msg=k)
     assert rel_frob(got["tile_valC"], z["tile_valC"]) <= 1e-12
+
+
+@pytest.mark.parametrize("name,a", [("stencil27_8", synth.stencil27_dof3(8)), ("dense_tile", cases.dense_tile_csr(np.float32)),
+                                    ("rmat_12", synth.rmat(12, 16)), ("poisson2d_64", synth.poisson2d(64, np.float32))])
+def test_mixed_precision_tensor_path(handle, name, a):
+    """Dense tile pairs on tensor cores (FP16 hi+lo, FP32 accumulation): exact
+    structure, <= 1e-6 relative Frobenius error against the FP64 oracle."""
+    got, S = check_product(handle, a, a, "plain", np.float32, prec="mixed")
+    st = handle.stats()
+    if name in ("stencil27_8", "dense_tile"):
+        assert st["tensor_pairs"] > 0
