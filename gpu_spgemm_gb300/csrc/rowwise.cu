@@ -33,8 +33,8 @@ constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
 constexpr int NW_MAXT = 1024;   // C tiles per numeric window
 constexpr int NW_VALS = 8192;   // C values per numeric window
-constexpr int MAXA_SMEM = 1024; // A nonzeros per tile-row whose cursors fit in shared memory
-constexpr int HEAVY = 64;       // B rows longer than this are walked by a whole warp
+constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose walk state fits in shared memory
+constexpr int WCHUNK = 4;       // products per thread between searches in the flattened walk
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
     while (lo < hi) {
@@ -191,80 +191,90 @@ __device__ __forceinline__ int row_of(const int* s_rows, int e) {
     return r;
 }
 
+// Per-window scratch of the load-balanced walk: for every A nonzero of the
+// tile-row its B-row segment inside the window (start) and the exclusive
+// prefix of the segment lengths (off).  Shared memory for tile-rows with at
+// most MAXA_SMEM nonzeros, a global slice otherwise.
+struct WalkBuf {
+    int* start;
+    int* off;
+    uint8_t* row;
+};
+
 // Runs `op(x, r, p, c)` for every B entry (position p, column c < limit) that
-// the A nonzeros of the tile-row reach inside the current window, advancing
-// each nonzero's cursor past the window.  Each warp takes 32 A nonzeros at a
-// time, one per lane.  A lane whose B row is short (<= HEAVY entries in all)
-// walks its few entries in this window alone; the lanes whose B row is long
-// (the hub rows of a power-law matrix) are then taken one at a time by the
-// whole warp, which reads 128 entries per round trip (four independent loads
-// per lane) so the walk is bound by throughput, not by load latency.  No
-// queue, no second pass.  `op` is called with the A-nonzero index x.
+// the A nonzeros of the tile-row reach inside the current window, and moves
+// each nonzero's cursor past the window.  Load-balanced expansion:
+//   1. one thread per A nonzero finds the end of its segment in this window
+//      (galloping search from the cursor; most segments on power-law
+//      matrices are 0-2 entries long) and records its length;
+//   2. a block-wide exclusive scan of the lengths;
+//   3. all threads sweep the flattened products in contiguous chunks of
+//      WCHUNK, one binary search per chunk to find the owning nonzero, so
+//      every product is an independent load + op: no serial dependency
+//      chains and no idle lanes, however skewed the segment lengths are.
 template <typename Op>
 __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const int* s_rows, int limit,
                                             const int* __restrict__ a_ci, const int* __restrict__ b_rp,
-                                            const int* __restrict__ b_ci, Op op) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int base = warp * 32; base < it.na; base += RW_THREADS) {
-        const int x = base + lane;
-        int2 cs = make_int2(0, INT_MAX);
-        int k = 0, bs = 0, be = 0;
-        if (x < it.na) {
-            cs = cur[x];
-            if (cs.y < limit) {
-                k = __ldg(&a_ci[it.e0 + x]);
-                bs = __ldg(&b_rp[k]);
-                be = __ldg(&b_rp[k + 1]);
-            }
-        }
-        const bool has = cs.y < limit;
-        const bool heavy = has && (be - bs) > HEAVY;
-        const int r = has ? row_of(s_rows, it.e0 + x) : 0;
-        if (has && !heavy) {
-            int p = cs.x, c = cs.y;
-            while (c < limit) {
-                const int cn = (p + 1 < be) ? __ldg(&b_ci[p + 1]) : INT_MAX;  // next column, loaded early
-                op(x, r, p, c);
-                p++;
-                c = cn;
-            }
-            cur[x] = make_int2(p, c);
-        }
-        unsigned hm = __ballot_sync(0xffffffffu, heavy);
-        while (hm) {
-            const int src = __ffs(hm) - 1;
-            hm &= hm - 1u;
-            const int hx = base + src;
-            const int hr = __shfl_sync(0xffffffffu, r, src);
-            const int hbe = __shfl_sync(0xffffffffu, be, src);
-            int p = __shfl_sync(0xffffffffu, cs.x, src), nextc = INT_MAX;
+                                            const int* __restrict__ b_ci, WalkBuf wb, int64_t* s_sh, Op op) {
+    const int tid = threadIdx.x;
+    // 1. segment ends; blocked assignment so the scan below is contiguous
+    const int per = (it.na + RW_THREADS - 1) / RW_THREADS;
+    const int x0 = min(it.na, tid * per), x1 = min(it.na, x0 + per);
+    int64_t local = 0;
+    for (int x = x0; x < x1; x++) {
+        const int2 cs = cur[x];
+        int len = 0;
+        if (cs.y < limit) {
+            const int k = __ldg(&a_ci[it.e0 + x]);
+            const int be = __ldg(&b_rp[k + 1]);
+            // gallop: last position known < limit is lo, first probe >= limit is hi
+            int lo = cs.x, step = 1, hi = be;
             while (true) {
-                int cc[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int q = p + 32 * u + lane;
-                    cc[u] = q < hbe ? __ldg(&b_ci[q]) : INT_MAX;
-                }
-                int n = 0;
-                bool stop = false;
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const bool in = cc[u] < limit;
-                    if (in) op(hx, hr, p + 32 * u + lane, cc[u]);
-                    const unsigned bal = __ballot_sync(0xffffffffu, in);
-                    const int nu = __popc(bal);
-                    if (!stop && nu < 32) {
-                        nextc = __shfl_sync(0xffffffffu, cc[u], nu);
-                        n += nu;
-                        stop = true;
-                    } else if (!stop) {
-                        n += 32;
-                    }
-                }
-                p += n;
-                if (stop) break;
+                const int q = lo + step;
+                if (q >= be) { hi = be; break; }
+                if (__ldg(&b_ci[q]) >= limit) { hi = q; break; }
+                lo = q;
+                step <<= 1;
             }
-            if (lane == 0) cur[hx] = make_int2(p, nextc);
+            while (hi - lo > 1) {  // b_ci[lo] < limit <= b_ci[hi] (or hi == be)
+                const int mid = (lo + hi) >> 1;
+                if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
+            }
+            len = hi - cs.x;
+            cur[x] = make_int2(hi, hi < be ? __ldg(&b_ci[hi]) : INT_MAX);
+        }
+        wb.start[x] = cs.x;
+        wb.off[x] = len;
+        wb.row[x] = (uint8_t)row_of(s_rows, it.e0 + x);
+        local += len;
+    }
+    // 2. exclusive scan of the lengths
+    int64_t total;
+    int64_t run = block_excl_scan<int64_t>(local, s_sh, &total);
+    for (int x = x0; x < x1; x++) {
+        const int l = wb.off[x];
+        wb.off[x] = (int)run;
+        run += l;
+    }
+    __syncthreads();
+    // 3. flattened products in contiguous chunks
+    const int P = (int)total;
+    for (int q0 = tid * WCHUNK; q0 < P; q0 += RW_THREADS * WCHUNK) {
+        const int q1 = min(P, q0 + WCHUNK);
+        int lo = 0, hi = it.na;  // last x with off[x] <= q0
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (wb.off[mid] <= q0) lo = mid; else hi = mid;
+        }
+        int x = lo;
+        int next = (x + 1 < it.na) ? wb.off[x + 1] : P;
+        for (int q = q0; q < q1; q++) {
+            while (q >= next) {
+                x++;
+                next = (x + 1 < it.na) ? wb.off[x + 1] : P;
+            }
+            const int p = wb.start[x] + (q - wb.off[x]);
+            op(x, (int)wb.row[x], p, __ldg(&b_ci[p]));
         }
     }
     __syncthreads();
@@ -278,11 +288,15 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                    const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                    const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                    const int* __restrict__ b_ci, uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC,
-                   int* __restrict__ tile_cnt, unsigned long long* ticket, int2* __restrict__ cursor_g, int max_na) {
+                   int* __restrict__ tile_cnt, unsigned long long* ticket, int2* __restrict__ cursor_g, int* __restrict__ walk_g,
+                   int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* masks32 = smem;                      // [16][WS] halfwords
     int2* cur_s = reinterpret_cast<int2*>(masks32 + WS * 8);
-    uint32_t* bm = reinterpret_cast<uint32_t*>(cur_s + MAXA_SMEM);
+    int* wstart_s = reinterpret_cast<int*>(cur_s + MAXA_SMEM);
+    int* woff_s = wstart_s + MAXA_SMEM;
+    uint8_t* wrow_s = reinterpret_cast<uint8_t*>(woff_s + MAXA_SMEM);
+    uint32_t* bm = reinterpret_cast<uint32_t*>(wrow_s + MAXA_SMEM);
     uint32_t* pre = bm + nwords_b;
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
@@ -291,7 +305,14 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
-        int2* cur = (it.na <= MAXA_SMEM) ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        const bool in_smem = it.na <= MAXA_SMEM;
+        int2* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        WalkBuf wb;
+        if (in_smem) { wb.start = wstart_s; wb.off = woff_s; wb.row = wrow_s; }
+        else {
+            int* g = walk_g + (int64_t)blockIdx.x * max_na * 3;
+            wb.start = g; wb.off = g + max_na; wb.row = reinterpret_cast<uint8_t*>(g + 2 * (int64_t)max_na);
+        }
         init_cursors(it, cur, colidxC, a_ci, b_rp, b_ci);
         for (int w0 = it.rs; w0 < it.re; w0 += WS) {
             const int nt = min(WS, it.re - w0);
@@ -300,7 +321,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci,
+            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, wb, s_sh,
                         [&](int, int r, int, int c) {
                             const int lt = wrank(bm, pre, wlo, c >> 4);
                             const int idx = r * WS + lt;
@@ -344,14 +365,17 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   const uint8_t* __restrict__ ptrRowC, const int* __restrict__ a_rp, const int* __restrict__ a_ci,
                   const V* __restrict__ a_val, const int* __restrict__ b_rp, const int* __restrict__ b_ci,
                   const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
-                  unsigned long long* ticket, int2* __restrict__ cursor_g, int max_na) {
+                  unsigned long long* ticket, int2* __restrict__ cursor_g, int* __restrict__ walk_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     ACC* acc = reinterpret_cast<ACC*>(smem);                                   // NW_VALS + 256
     uint16_t* mk = reinterpret_cast<uint16_t*>(acc + NW_VALS + 256);           // [NW_MAXT][16]
     uint8_t* pr = reinterpret_cast<uint8_t*>(mk + NW_MAXT * TS);               // [NW_MAXT][16]
     int* vbase = reinterpret_cast<int*>(pr + NW_MAXT * TS);                    // NW_MAXT
     int2* cur_s = reinterpret_cast<int2*>(vbase + NW_MAXT);                    // MAXA_SMEM
-    uint32_t* bm = reinterpret_cast<uint32_t*>(cur_s + MAXA_SMEM);
+    int* wstart_s = reinterpret_cast<int*>(cur_s + MAXA_SMEM);
+    int* woff_s = wstart_s + MAXA_SMEM;
+    uint8_t* wrow_s = reinterpret_cast<uint8_t*>(woff_s + MAXA_SMEM);
+    uint32_t* bm = reinterpret_cast<uint32_t*>(wrow_s + MAXA_SMEM);
     uint32_t* pre = bm + nwords_b;
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
@@ -361,7 +385,14 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
-        int2* cur = (it.na <= MAXA_SMEM) ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        const bool in_smem = it.na <= MAXA_SMEM;
+        int2* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        WalkBuf wb;
+        if (in_smem) { wb.start = wstart_s; wb.off = woff_s; wb.row = wrow_s; }
+        else {
+            int* g = walk_g + (int64_t)blockIdx.x * max_na * 3;
+            wb.start = g; wb.off = g + max_na; wb.row = reinterpret_cast<uint8_t*>(g + 2 * (int64_t)max_na);
+        }
         init_cursors(it, cur, colidxC, a_ci, b_rp, b_ci);
         int t0 = it.rs;
         while (t0 < it.re) {
@@ -396,7 +427,7 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci,
+            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, wb, s_sh,
                         [&](int x, int r, int p, int c) {
                             const int lt = wrank(bm, pre, wlo, c >> 4);
                             const uint32_t m16 = mk[lt * TS + r];
@@ -422,13 +453,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 }
 
 size_t sym_smem(int nwords_b) {
-    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * 8 + 2 * (size_t)nwords_b * 4;
+    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * (8 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
 }
 
 template <typename ACC>
 size_t num_smem(int nwords_b) {
     return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 2 + (size_t)NW_MAXT * TS +
-           (size_t)NW_MAXT * 4 + (size_t)MAXA_SMEM * 8 + 2 * (size_t)nwords_b * 4;
+           (size_t)NW_MAXT * 4 + (size_t)MAXA_SMEM * (8 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
 }
 
 }  // namespace
@@ -482,6 +513,7 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
     rp->grid = h->num_sms * 4;
     if (rp->max_na > MAXA_SMEM) {
         SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na + 1));
+        SPG_TRY(spg_alloc_t(h, &rp->walk_g, (size_t)rp->grid * rp->max_na * 3 + 1));
     }
     return SPG_OK;
 }
@@ -501,7 +533,7 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
     rw_symbolic_kernel<<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, A->row_ptr,
-        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na);
+        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->walk_g, rp->max_na);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }
@@ -521,7 +553,8 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
     rw_numeric_kernel<V, ACC><<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
-        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na);
+        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->walk_g,
+        rp->max_na);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }
@@ -546,6 +579,7 @@ void rowwise_free_priv(spg_handle_t h, RowwisePriv* rp) {
     spg_free_async(h, rp->item_prefix);
     spg_free_async(h, rp->counters);
     spg_free_async(h, rp->cursor_g);
+    spg_free_async(h, rp->walk_g);
     *rp = RowwisePriv{};
 }
 

@@ -75,7 +75,7 @@ struct spg_handle_s {
     struct spg_mlp_s* sizing = nullptr;  // learned sizing model (optional)
     float sizing_margin = 0.25f;
     int dense_thr = 32;        // tile nnz above which a tile pair goes to tensor cores (MIXED)
-    float cancel_eps = 1e-3f;  // |c| < eps * sum|a||b| flags a C tile for FP64 recomputation
+    float cancel_eps = 9.5367431640625e-07f;  // 2^-20: |c| < eps * sum|a||b| flags a C tile for FP64
     cudaStream_t stream = nullptr;
     std::string err;
     spg_stats stats{};
