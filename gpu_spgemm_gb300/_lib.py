@@ -69,6 +69,7 @@ SIGNATURES = {
     "spg_products": (I32, [P, C.POINTER(SpgTiles), C.POINTER(SpgTiles), C.POINTER(I64)]),
     "spg_csr_transpose": (I32, [P, I32, I32, I64, P, P, P, I32, P, P, P]),
     "spg_ctiles_to_csr": (I32, [P, C.POINTER(SpgCTiles), P, P, P, C.POINTER(I64)]),
+    "spg_ctiles_to_csr_noalloc": (I32, [P, C.POINTER(SpgCTiles), P, P, P, C.POINTER(I64)]),
     "spg_batch_create_host": (I32, [P, I32, P, P, P, P, P, P, P, P, P, P, P, I32, C.POINTER(P)]),
     "spg_batch_free": (I32, [P, P]),
     "spg_batch_spgemm": (I32, [P, P, I32, I32]),

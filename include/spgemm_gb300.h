@@ -229,6 +229,22 @@ spg_status spg_csr_transpose(spg_handle_t h, int m, int n, int64_t nnz, const in
 spg_status spg_ctiles_to_csr(spg_handle_t h, const spg_ctiles* C, int* out_rp, int* out_ci, void* out_val,
                              int64_t* nnz);
 
+/* C's tiles -> device CSR like spg_ctiles_to_csr, but the library allocates
+   no device memory at all.  No counterpart in the reference (which owns all
+   its buffers).  For callers that cannot let a library allocate: a serving
+   process or host framework that owns every byte of HBM through its own pool,
+   code where an allocation could block or fail at an unpredictable time, a
+   plugin handed only a stream and buffers.  The caller passes the outputs
+   (out_rp: m+1 ints, out_ci / out_val: C->nnzC entries); the working memory
+   is a fixed area inside the library (a static device array of about 4 MiB,
+   held on every GPU that loads the library until the process exits), so C may
+   have at most 1,048,576 rows; more returns SPG_ERR_INVALID.  The first call
+   on a device looks up that area's address, so make it before any stream
+   capture.  All calls share the area: calls whose work overlaps on the GPU
+   race on it, so order them on one stream. *nnz receives C->nnzC. */
+spg_status spg_ctiles_to_csr_noalloc(spg_handle_t h, const spg_ctiles* C, int* out_rp, int* out_ci,
+                                     void* out_val, int64_t* nnz);
+
 /* Galerkin triple product RAP = P^T (A P) on the device (no reference
    counterpart; it chains two of the reference's SpGEMMs): A (m x m) and P
    (m x nc) are device CSR; A*P is formed, converted to CSR and re-tiled as the
