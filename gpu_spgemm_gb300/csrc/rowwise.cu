@@ -34,7 +34,7 @@ constexpr int WS = 2048;        // C tiles per symbolic window
 constexpr int NW_MAXT = 1024;   // C tiles per numeric window
 constexpr int NW_VALS = 8192;   // C values per numeric window
 constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose walk state fits in shared memory
-constexpr int WCHUNK = 4;       // products per thread between searches in the flattened walk
+constexpr int WCHUNK = 8;       // products per thread per step of the flattened walk (loads in flight)
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
     while (lo < hi) {
@@ -140,8 +140,9 @@ __device__ bool next_item(unsigned long long* ticket, const int64_t* __restrict_
 }
 
 // Cursor of every A nonzero of the tile-row: first B-row position whose column
-// is >= the region's first column, and that column (INT_MAX past the row end).
-__device__ void init_cursors(const ItemInfo& it, int2* cur, const int* __restrict__ colidxC,
+// is >= the region's first column, that column (INT_MAX past the row end),
+// and the row's end (so later windows need no a_ci / b_rp loads).
+__device__ void init_cursors(const ItemInfo& it, int4* cur, const int* __restrict__ colidxC,
                              const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                              const int* __restrict__ b_ci) {
     const int cstart = colidxC[it.rs] * TS;
@@ -150,7 +151,7 @@ __device__ void init_cursors(const ItemInfo& it, int2* cur, const int* __restric
         int b = __ldg(&b_rp[k]);
         const int be = __ldg(&b_rp[k + 1]);
         if (it.q > 0) b = lower_bound_i(b_ci, b, be, cstart);
-        cur[x] = make_int2(b, b < be ? __ldg(&b_ci[b]) : INT_MAX);
+        cur[x] = make_int4(b, b < be ? __ldg(&b_ci[b]) : INT_MAX, be, 0);
     }
     __syncthreads();
 }
@@ -213,8 +214,7 @@ struct WalkBuf {
 //      every product is an independent load + op: no serial dependency
 //      chains and no idle lanes, however skewed the segment lengths are.
 template <typename Op>
-__device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const int* s_rows, int limit,
-                                            const int* __restrict__ a_ci, const int* __restrict__ b_rp,
+__device__ __forceinline__ void walk_window(const ItemInfo& it, int4* cur, const int* s_rows, int limit,
                                             const int* __restrict__ b_ci, WalkBuf wb, int64_t* s_sh, Op op) {
     const int tid = threadIdx.x;
     // 1. segment ends; blocked assignment so the scan below is contiguous
@@ -222,11 +222,10 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const
     const int x0 = min(it.na, tid * per), x1 = min(it.na, x0 + per);
     int64_t local = 0;
     for (int x = x0; x < x1; x++) {
-        const int2 cs = cur[x];
+        const int4 cs = cur[x];
         int len = 0;
         if (cs.y < limit) {
-            const int k = __ldg(&a_ci[it.e0 + x]);
-            const int be = __ldg(&b_rp[k + 1]);
+            const int be = cs.z;
             // gallop: last position known < limit is lo, first probe >= limit is hi
             int lo = cs.x, step = 1, hi = be;
             while (true) {
@@ -241,7 +240,7 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const
                 if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
             }
             len = hi - cs.x;
-            cur[x] = make_int2(hi, hi < be ? __ldg(&b_ci[hi]) : INT_MAX);
+            cur[x] = make_int4(hi, hi < be ? __ldg(&b_ci[hi]) : INT_MAX, be, 0);
         }
         wb.start[x] = cs.x;
         wb.off[x] = len;
@@ -257,10 +256,10 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const
         run += l;
     }
     __syncthreads();
-    // 3. flattened products in contiguous chunks
+    // 3. flattened products in contiguous chunks of WCHUNK: positions first,
+    //    then every load of the chunk in flight at once, then the products
     const int P = (int)total;
     for (int q0 = tid * WCHUNK; q0 < P; q0 += RW_THREADS * WCHUNK) {
-        const int q1 = min(P, q0 + WCHUNK);
         int lo = 0, hi = it.na;  // last x with off[x] <= q0
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
@@ -268,17 +267,78 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, int2* cur, const
         }
         int x = lo;
         int next = (x + 1 < it.na) ? wb.off[x + 1] : P;
-        for (int q = q0; q < q1; q++) {
-            while (q >= next) {
-                x++;
-                next = (x + 1 < it.na) ? wb.off[x + 1] : P;
+        int px[WCHUNK], pp[WCHUNK];
+#pragma unroll
+        for (int u = 0; u < WCHUNK; u++) {
+            const int q = q0 + u;
+            if (q < P) {
+                while (q >= next) {
+                    x++;
+                    next = (x + 1 < it.na) ? wb.off[x + 1] : P;
+                }
+                px[u] = x;
+                pp[u] = wb.start[x] + (q - wb.off[x]);
+            } else {
+                px[u] = -1;
+                pp[u] = 0;
             }
-            const int p = wb.start[x] + (q - wb.off[x]);
-            op(x, (int)wb.row[x], p, __ldg(&b_ci[p]));
         }
+        typename Op::Loaded ld[WCHUNK];
+        int cc[WCHUNK];
+#pragma unroll
+        for (int u = 0; u < WCHUNK; u++) {
+            cc[u] = px[u] >= 0 ? __ldg(&b_ci[pp[u]]) : 0;
+            ld[u] = op.load(px[u], pp[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < WCHUNK; u++)
+            if (px[u] >= 0) op.apply(px[u], (int)wb.row[px[u]], cc[u], ld[u]);
     }
     __syncthreads();
 }
+
+// Symbolic product: OR the column's bit into C's row mask.
+struct SymOp {
+    struct Loaded {};
+    const uint32_t* bm;
+    const uint32_t* pre;
+    int wlo;
+    uint32_t* masks32;
+    __device__ __forceinline__ Loaded load(int, int) const { return Loaded{}; }
+    __device__ __forceinline__ void apply(int, int r, int c, Loaded) const {
+        const int lt = wrank(bm, pre, wlo, c >> 4);
+        const int idx = r * WS + lt;
+        atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
+    }
+};
+
+// Numeric product: a_ik * b_kc into C's value slot.
+template <typename V, typename ACC>
+struct NumOp {
+    struct Loaded { ACC va, vb; };
+    const uint32_t* bm;
+    const uint32_t* pre;
+    int wlo;
+    const uint16_t* mk;
+    const uint8_t* pr;
+    const int* vbase;
+    ACC* acc;
+    const V* a_val;
+    const V* b_val;
+    int e0;
+    __device__ __forceinline__ Loaded load(int x, int p) const {
+        Loaded l;
+        l.va = x >= 0 ? (ACC)__ldg(&a_val[e0 + x]) : ACC(0);
+        l.vb = x >= 0 ? (ACC)__ldg(&b_val[p]) : ACC(0);
+        return l;
+    }
+    __device__ __forceinline__ void apply(int, int r, int c, Loaded l) const {
+        const int lt = wrank(bm, pre, wlo, c >> 4);
+        const uint32_t m16 = mk[lt * TS + r];
+        const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
+        atomicAdd(&acc[pos], l.va * l.vb);
+    }
+};
 
 // ---------------------------------------------------------------------------
 // symbolic
@@ -288,11 +348,11 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                    const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                    const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                    const int* __restrict__ b_ci, uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC,
-                   int* __restrict__ tile_cnt, unsigned long long* ticket, int2* __restrict__ cursor_g, int* __restrict__ walk_g,
+                   int* __restrict__ tile_cnt, unsigned long long* ticket, int4* __restrict__ cursor_g, int* __restrict__ walk_g,
                    int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* masks32 = smem;                      // [16][WS] halfwords
-    int2* cur_s = reinterpret_cast<int2*>(masks32 + WS * 8);
+    int4* cur_s = reinterpret_cast<int4*>(masks32 + WS * 8);
     int* wstart_s = reinterpret_cast<int*>(cur_s + MAXA_SMEM);
     int* woff_s = wstart_s + MAXA_SMEM;
     uint8_t* wrow_s = reinterpret_cast<uint8_t*>(woff_s + MAXA_SMEM);
@@ -306,7 +366,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
         const bool in_smem = it.na <= MAXA_SMEM;
-        int2* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        int4* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
         WalkBuf wb;
         if (in_smem) { wb.start = wstart_s; wb.off = woff_s; wb.row = wrow_s; }
         else {
@@ -321,12 +381,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, wb, s_sh,
-                        [&](int, int r, int, int c) {
-                            const int lt = wrank(bm, pre, wlo, c >> 4);
-                            const int idx = r * WS + lt;
-                            atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
-                        });
+            walk_window(it, cur, s_rows, limit, b_ci, wb, s_sh, SymOp{bm, pre, wlo, masks32});
             for (int x = tid; x < nt; x += RW_THREADS) {
                 uint32_t mw[8];
                 uint32_t pw[4] = {0u, 0u, 0u, 0u};
@@ -365,13 +420,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   const uint8_t* __restrict__ ptrRowC, const int* __restrict__ a_rp, const int* __restrict__ a_ci,
                   const V* __restrict__ a_val, const int* __restrict__ b_rp, const int* __restrict__ b_ci,
                   const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
-                  unsigned long long* ticket, int2* __restrict__ cursor_g, int* __restrict__ walk_g, int max_na) {
+                  unsigned long long* ticket, int4* __restrict__ cursor_g, int* __restrict__ walk_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     ACC* acc = reinterpret_cast<ACC*>(smem);                                   // NW_VALS + 256
     uint16_t* mk = reinterpret_cast<uint16_t*>(acc + NW_VALS + 256);           // [NW_MAXT][16]
     uint8_t* pr = reinterpret_cast<uint8_t*>(mk + NW_MAXT * TS);               // [NW_MAXT][16]
     int* vbase = reinterpret_cast<int*>(pr + NW_MAXT * TS);                    // NW_MAXT
-    int2* cur_s = reinterpret_cast<int2*>(vbase + NW_MAXT);                    // MAXA_SMEM
+    int4* cur_s = reinterpret_cast<int4*>(vbase + NW_MAXT);                    // MAXA_SMEM
     int* wstart_s = reinterpret_cast<int*>(cur_s + MAXA_SMEM);
     int* woff_s = wstart_s + MAXA_SMEM;
     uint8_t* wrow_s = reinterpret_cast<uint8_t*>(woff_s + MAXA_SMEM);
@@ -386,7 +441,7 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
         const bool in_smem = it.na <= MAXA_SMEM;
-        int2* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
+        int4* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
         WalkBuf wb;
         if (in_smem) { wb.start = wstart_s; wb.off = woff_s; wb.row = wrow_s; }
         else {
@@ -427,14 +482,8 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, a_ci, b_rp, b_ci, wb, s_sh,
-                        [&](int x, int r, int p, int c) {
-                            const int lt = wrank(bm, pre, wlo, c >> 4);
-                            const uint32_t m16 = mk[lt * TS + r];
-                            const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
-                            acc_add(&acc[pos], (ACC)__ldg(&a_val[it.e0 + x]) * (ACC)__ldg(&b_val[p]));
-                        });
-            __syncthreads();
+            walk_window(it, cur, s_rows, limit, b_ci, wb, s_sh,
+                        NumOp<V, ACC>{bm, pre, wlo, mk, pr, vbase, acc, a_val, b_val, it.e0});
             for (int x = tid; x < nv; x += RW_THREADS) valC[v0 + x] = (V)acc[x];
             for (int x = tid; x < ntw * TS; x += RW_THREADS) {
                 const int lt = x >> 4, r = x & 15;
@@ -453,13 +502,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 }
 
 size_t sym_smem(int nwords_b) {
-    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * (8 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
+    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * (16 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
 }
 
 template <typename ACC>
 size_t num_smem(int nwords_b) {
     return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 2 + (size_t)NW_MAXT * TS +
-           (size_t)NW_MAXT * 4 + (size_t)MAXA_SMEM * (8 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
+           (size_t)NW_MAXT * 4 + (size_t)MAXA_SMEM * (16 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
 }
 
 }  // namespace
@@ -512,7 +561,7 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
     // memory: one slice per resident CTA (<= 4 CTAs of 512 threads per SM)
     rp->grid = h->num_sms * 4;
     if (rp->max_na > MAXA_SMEM) {
-        SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na + 1));
+        SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na + 1));  // int4 each
         SPG_TRY(spg_alloc_t(h, &rp->walk_g, (size_t)rp->grid * rp->max_na * 3 + 1));
     }
     return SPG_OK;
