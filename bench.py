@@ -201,6 +201,10 @@ def run_ours(args):
     B = api.build_csc_tiles(h, b)
     products = api.products(h, A, B)
     flops = 2.0 * products
+    sizing = None
+    if args.sizing and os.path.exists(api.SIZING_MODEL_PATH):
+        sizing = api.SizingModel.load(h)
+        sizing.attach(args.sizing_margin)
 
     def step():
         C = api.spgemm(h, A, B, algo=args.algo, prec=args.prec)
@@ -294,6 +298,12 @@ def run_ours(args):
                     "ms_step1": s1, "ms_step2": s2, "ms_step3": s3,
                     "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak,
                     "tensor_pairs": stats[-1].get("tensor_pairs", 0), "fp64_tiles": stats[-1].get("fp64_tiles", 0),
+                    "learned_sizing": None if sizing is None else {
+                        "model": os.path.relpath(api.SIZING_MODEL_PATH, ROOT), "margin": args.sizing_margin,
+                        "predicted_tiles": stats[-1].get("predicted_tiles", 0), "actual_tiles": numtileC,
+                        "overflow_reruns": stats[-1].get("overflow_reruns", 0),
+                        "step1": "one fused count+fill pass" if stats[-1].get("overflow_reruns", 0) == 0
+                        else "fused pass + exact fill re-run"},
                     "accuracy": accuracy})
         line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -508,6 +518,8 @@ def main():
     p.add_argument("--ref-step-s", type=float, default=8.0)
     p.add_argument("--batch-count", type=int, default=512)
     p.add_argument("--check", action="store_true", help="value error vs the FP64 oracle on a prefix of C")
+    p.add_argument("--sizing", type=int, default=1, help="attach the trained sizing MLP (1) or not (0)")
+    p.add_argument("--sizing-margin", type=float, default=0.25)
     p.add_argument("--traffic", type=float, default=None,
                    help="dram bytes per launch of the dominant kernel from an ncu capture")
     args = p.parse_args()
