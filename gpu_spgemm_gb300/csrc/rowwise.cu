@@ -31,9 +31,11 @@ constexpr int RW_THREADS = 512;
 constexpr int RW_WARPS = RW_THREADS / 32;
 constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
-constexpr int NW_MAXT = 1024;   // C tiles per numeric window
-constexpr int NW_VALS = 8192;   // C values per numeric window
-constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose walk state fits in shared memory
+constexpr int NW_MAXT = 768;    // C tiles per numeric window
+constexpr int NW_VALS = 6144;   // C values per numeric window
+constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose cursors fit in shared memory
+constexpr int AL = 1024;        // segments per list of the walk (shared memory)
+constexpr int FU = AL / RW_THREADS;  // A nonzeros per thread per filter step
 constexpr int WCHUNK = 8;       // products per thread per step of the flattened walk (loads in flight)
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
@@ -139,10 +141,25 @@ __device__ bool next_item(unsigned long long* ticket, const int64_t* __restrict_
     return true;
 }
 
+// Walk state of the A nonzeros of a tile-row, one array per field: the
+// cursor into the nonzero's B row, the column there (INT_MAX past the row
+// end), the row's end, and the length of the nonzero's latest segment (the
+// first guess for its next one).
+struct Cursors {
+    int* pos;
+    int* col;
+    int* end;
+    int* len;
+};
+
+__device__ __forceinline__ Cursors cursors_at(int* base, int stride) {
+    return Cursors{base, base + stride, base + 2 * stride, base + 3 * stride};
+}
+
 // Cursor of every A nonzero of the tile-row: first B-row position whose column
-// is >= the region's first column, that column (INT_MAX past the row end),
-// and the row's end (so later windows need no a_ci / b_rp loads).
-__device__ void init_cursors(const ItemInfo& it, int4* cur, const int* __restrict__ colidxC,
+// is >= the region's first column, that column, and the row's end (so later
+// windows need no a_ci / b_rp loads).
+__device__ void init_cursors(const ItemInfo& it, Cursors cu, const int* __restrict__ colidxC,
                              const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                              const int* __restrict__ b_ci) {
     const int cstart = colidxC[it.rs] * TS;
@@ -151,7 +168,10 @@ __device__ void init_cursors(const ItemInfo& it, int4* cur, const int* __restric
         int b = __ldg(&b_rp[k]);
         const int be = __ldg(&b_rp[k + 1]);
         if (it.q > 0) b = lower_bound_i(b_ci, b, be, cstart);
-        cur[x] = make_int4(b, b < be ? __ldg(&b_ci[b]) : INT_MAX, be, 0);
+        cu.pos[x] = b;
+        cu.col[x] = b < be ? __ldg(&b_ci[b]) : INT_MAX;
+        cu.end[x] = be;
+        cu.len[x] = 0;
     }
     __syncthreads();
 }
@@ -192,94 +212,148 @@ __device__ __forceinline__ int row_of(const int* s_rows, int e) {
     return r;
 }
 
-// Per-window scratch of the load-balanced walk: for every A nonzero of the
-// tile-row its B-row segment inside the window (start) and the exclusive
-// prefix of the segment lengths (off).  Shared memory for tile-rows with at
-// most MAXA_SMEM nonzeros, a global slice otherwise.
-struct WalkBuf {
+// Segment list of the walk, in shared memory: entry k is A nonzero ax[k]
+// (row row[k] of the tile-row) with the B positions [start[k], start[k] +
+// off[k+1] - off[k]) below the window's limit; off[] is the exclusive prefix
+// of the segment lengths, off[K] the list's total.
+struct SegList {
+    int* ax;
     int* start;
-    int* off;
+    int* off;  // AL + 1
     uint8_t* row;
 };
 
-// Runs `op(x, r, p, c)` for every B entry (position p, column c < limit) that
-// the A nonzeros of the tile-row reach inside the current window, and moves
-// each nonzero's cursor past the window.  Load-balanced expansion:
-//   1. one thread per A nonzero finds the end of its segment in this window
-//      (galloping search from the cursor; most segments on power-law
-//      matrices are 0-2 entries long) and records its length;
+// ax, start: AL ints each; off: AL + 4 ints (keeps 16-byte alignment); row: AL bytes
+constexpr size_t SEGLIST_BYTES = (size_t)AL * 4 * 3 + 16 + AL;
+
+__device__ __forceinline__ SegList seglist_at(int* base) {
+    return SegList{base, base + AL, base + 2 * AL, reinterpret_cast<uint8_t*>(base + 3 * AL + 4)};
+}
+
+// Segment end of one listed nonzero: the first position >= p0 + 1 whose
+// column reaches `limit` (b_ci[p0] < limit is known).  The guess g (the
+// nonzero's previous segment length) is probed first together with its
+// successor, so a repeat of the last length costs one round of loads; a
+// shorter segment is found by bisection below the guess, a longer one by
+// galloping above it.  Returns the end; *nc receives the column there.
+__device__ __forceinline__ int segment_end(const int* __restrict__ b_ci, int p0, int be, int g, int pa, int pb,
+                                           int limit, int* nc) {
+    if (pa >= limit) {  // b_ci[p0] < limit <= b_ci[p0 + g - 1]
+        int lo = p0, hi = p0 + g - 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
+        }
+        *nc = (hi == p0 + g - 1) ? pa : __ldg(&b_ci[hi]);
+        return hi;
+    }
+    if (pb >= limit) {  // exactly g entries (pb is INT_MAX at the row end)
+        *nc = pb;
+        return p0 + g;
+    }
+    int lo = p0 + g, hi = be, step = g;  // b_ci[lo] = pb < limit
+    while (true) {
+        const int q = lo + step;
+        if (q >= be) break;
+        if (__ldg(&b_ci[q]) >= limit) { hi = q; break; }
+        lo = q;
+        step <<= 1;
+    }
+    while (hi - lo > 1) {  // b_ci[lo] < limit <= b_ci[hi] (or hi == be)
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
+    }
+    *nc = hi < be ? __ldg(&b_ci[hi]) : INT_MAX;
+    return hi;
+}
+
+// Runs `op` for every B entry of the K listed nonzeros' segments:
+//   1. each listed nonzero's segment end (segment_end), its cursor moved past
+//      the window;
 //   2. a block-wide exclusive scan of the lengths;
 //   3. all threads sweep the flattened products in contiguous chunks of
-//      WCHUNK, one binary search per chunk to find the owning nonzero, so
-//      every product is an independent load + op: no serial dependency
-//      chains and no idle lanes, however skewed the segment lengths are.
+//      WCHUNK, one binary search of off[] per chunk to find the owning
+//      segment, then every load of the chunk in flight at once, then the
+//      products: no serial dependency chains and no idle lanes, however
+//      skewed the segment lengths are.
 template <typename Op>
-__device__ __forceinline__ void walk_window(const ItemInfo& it, int4* cur, const int* s_rows, int limit,
-                                            const int* __restrict__ b_ci, WalkBuf wb, int64_t* s_sh, Op op) {
+__device__ __forceinline__ void run_list(const ItemInfo& it, Cursors cu, const int* s_rows, int limit,
+                                         const int* __restrict__ b_ci, SegList sl, int K, int64_t* s_sh, Op op) {
     const int tid = threadIdx.x;
-    // 1. segment ends; blocked assignment so the scan below is contiguous
-    const int per = (it.na + RW_THREADS - 1) / RW_THREADS;
-    const int x0 = min(it.na, tid * per), x1 = min(it.na, x0 + per);
-    int64_t local = 0;
-    for (int x = x0; x < x1; x++) {
-        const int4 cs = cur[x];
-        int len = 0;
-        if (cs.y < limit) {
-            const int be = cs.z;
-            // gallop: last position known < limit is lo, first probe >= limit is hi
-            int lo = cs.x, step = 1, hi = be;
-            while (true) {
-                const int q = lo + step;
-                if (q >= be) { hi = be; break; }
-                if (__ldg(&b_ci[q]) >= limit) { hi = q; break; }
-                lo = q;
-                step <<= 1;
-            }
-            while (hi - lo > 1) {  // b_ci[lo] < limit <= b_ci[hi] (or hi == be)
-                const int mid = (lo + hi) >> 1;
-                if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
-            }
-            len = hi - cs.x;
-            cur[x] = make_int4(hi, hi < be ? __ldg(&b_ci[hi]) : INT_MAX, be, 0);
+    // 1. segment ends: blocked assignment (<= FU entries a thread) so the
+    //    scan below is contiguous; every entry's loads are issued together
+    const int per = (K + RW_THREADS - 1) / RW_THREADS;
+    const int k0 = min(K, tid * per), k1 = min(K, k0 + per);
+    int xs[FU], p0[FU], be[FU], g[FU], pa[FU], pb[FU], ln[FU];
+#pragma unroll
+    for (int u = 0; u < FU; u++) {
+        const int k = k0 + u;
+        xs[u] = k < k1 ? sl.ax[k] : -1;
+        if (xs[u] >= 0) {
+            p0[u] = cu.pos[xs[u]];
+            be[u] = cu.end[xs[u]];
+            g[u] = cu.len[xs[u]];
         }
-        wb.start[x] = cs.x;
-        wb.off[x] = len;
-        wb.row[x] = (uint8_t)row_of(s_rows, it.e0 + x);
-        local += len;
+    }
+#pragma unroll
+    for (int u = 0; u < FU; u++) {
+        if (xs[u] >= 0) {
+            g[u] = max(1, min(g[u], be[u] - p0[u]));
+            pa[u] = g[u] > 1 ? __ldg(&b_ci[p0[u] + g[u] - 1]) : INT_MIN;
+            pb[u] = p0[u] + g[u] < be[u] ? __ldg(&b_ci[p0[u] + g[u]]) : INT_MAX;
+        }
+    }
+    int local = 0;
+#pragma unroll 1
+    for (int u = 0; u < FU; u++) {
+        ln[u] = 0;
+        if (xs[u] >= 0) {
+            int nc;
+            const int hi = segment_end(b_ci, p0[u], be[u], g[u], pa[u], pb[u], limit, &nc);
+            ln[u] = hi - p0[u];
+            cu.pos[xs[u]] = hi;
+            cu.col[xs[u]] = nc;
+            cu.len[xs[u]] = ln[u];
+            sl.start[k0 + u] = p0[u];
+            sl.row[k0 + u] = (uint8_t)row_of(s_rows, it.e0 + xs[u]);
+            local += ln[u];
+        }
     }
     // 2. exclusive scan of the lengths
     int64_t total;
-    int64_t run = block_excl_scan<int64_t>(local, s_sh, &total);
-    for (int x = x0; x < x1; x++) {
-        const int l = wb.off[x];
-        wb.off[x] = (int)run;
-        run += l;
-    }
+    int run = (int)block_excl_scan<int64_t>(local, s_sh, &total);
+#pragma unroll
+    for (int u = 0; u < FU; u++)
+        if (xs[u] >= 0) {
+            sl.off[k0 + u] = run;
+            run += ln[u];
+        }
+    const int P = (int)total;
+    if (tid == 0) sl.off[K] = P;
     __syncthreads();
     // 3. flattened products in contiguous chunks of WCHUNK: positions first,
     //    then every load of the chunk in flight at once, then the products
-    const int P = (int)total;
     for (int q0 = tid * WCHUNK; q0 < P; q0 += RW_THREADS * WCHUNK) {
-        int lo = 0, hi = it.na;  // last x with off[x] <= q0
+        int lo = 0, hi = K;  // last k with off[k] <= q0
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if (wb.off[mid] <= q0) lo = mid; else hi = mid;
+            if (sl.off[mid] <= q0) lo = mid; else hi = mid;
         }
-        int x = lo;
-        int next = (x + 1 < it.na) ? wb.off[x + 1] : P;
-        int px[WCHUNK], pp[WCHUNK];
+        int k = lo;
+        int next = sl.off[k + 1];
+        int pk[WCHUNK], pp[WCHUNK];
 #pragma unroll
         for (int u = 0; u < WCHUNK; u++) {
             const int q = q0 + u;
             if (q < P) {
-                while (q >= next) {
-                    x++;
-                    next = (x + 1 < it.na) ? wb.off[x + 1] : P;
+                while (q >= next) {  // every segment is non-empty: at most WCHUNK steps
+                    k++;
+                    next = sl.off[k + 1];
                 }
-                px[u] = x;
-                pp[u] = wb.start[x] + (q - wb.off[x]);
+                pk[u] = k;
+                pp[u] = sl.start[k] + (q - sl.off[k]);
             } else {
-                px[u] = -1;
+                pk[u] = -1;
                 pp[u] = 0;
             }
         }
@@ -287,14 +361,52 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, int4* cur, const
         int cc[WCHUNK];
 #pragma unroll
         for (int u = 0; u < WCHUNK; u++) {
-            cc[u] = px[u] >= 0 ? __ldg(&b_ci[pp[u]]) : 0;
-            ld[u] = op.load(px[u], pp[u]);
+            cc[u] = pk[u] >= 0 ? __ldg(&b_ci[pp[u]]) : 0;
+            ld[u] = op.load(pk[u] >= 0 ? sl.ax[pk[u]] : -1, pp[u]);
         }
 #pragma unroll
         for (int u = 0; u < WCHUNK; u++)
-            if (px[u] >= 0) op.apply(px[u], (int)wb.row[px[u]], cc[u], ld[u]);
+            if (pk[u] >= 0) op.apply(sl.row[pk[u]], cc[u], ld[u]);
     }
     __syncthreads();
+}
+
+// Runs `op(r, c, loaded)` for every B entry (column c < limit) that the A
+// nonzeros of the tile-row reach inside the current window, and moves each
+// nonzero's cursor past the window.  A filter pass reads only the cursor
+// columns (coalesced, FU per thread) and lists the nonzeros with an entry
+// below the limit; a full list of AL entries (or the last one) goes through
+// run_list.  Nonzeros with nothing in the window cost one 4-byte load.
+template <typename Op>
+__device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, const int* s_rows, int limit,
+                                            const int* __restrict__ b_ci, SegList sl, int64_t* s_sh, Op op) {
+    const int tid = threadIdx.x;
+    int K = 0;  // listed entries (block-uniform)
+    for (int f0 = 0; f0 < it.na; f0 += AL) {
+        int fx[FU];
+        int cnt = 0;
+#pragma unroll
+        for (int u = 0; u < FU; u++) {
+            const int x = f0 + u * RW_THREADS + tid;
+            fx[u] = (x < it.na && cu.col[x] < limit) ? x : -1;
+            cnt += fx[u] >= 0 ? 1 : 0;
+        }
+        int64_t tot;
+        int k = (int)block_excl_scan<int64_t>(cnt, s_sh, &tot);
+        if (K + (int)tot > AL) {
+            run_list(it, cu, s_rows, limit, b_ci, sl, K, s_sh, op);
+            K = 0;
+        }
+        k += K;
+#pragma unroll
+        for (int u = 0; u < FU; u++)
+            if (fx[u] >= 0) sl.ax[k++] = fx[u];
+        K += (int)tot;
+    }
+    if (K > 0) {
+        __syncthreads();
+        run_list(it, cu, s_rows, limit, b_ci, sl, K, s_sh, op);
+    }
 }
 
 // Symbolic product: OR the column's bit into C's row mask.
@@ -305,7 +417,7 @@ struct SymOp {
     int wlo;
     uint32_t* masks32;
     __device__ __forceinline__ Loaded load(int, int) const { return Loaded{}; }
-    __device__ __forceinline__ void apply(int, int r, int c, Loaded) const {
+    __device__ __forceinline__ void apply(int r, int c, Loaded) const {
         const int lt = wrank(bm, pre, wlo, c >> 4);
         const int idx = r * WS + lt;
         atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
@@ -332,7 +444,7 @@ struct NumOp {
         l.vb = x >= 0 ? (ACC)__ldg(&b_val[p]) : ACC(0);
         return l;
     }
-    __device__ __forceinline__ void apply(int, int r, int c, Loaded l) const {
+    __device__ __forceinline__ void apply(int r, int c, Loaded l) const {
         const int lt = wrank(bm, pre, wlo, c >> 4);
         const uint32_t m16 = mk[lt * TS + r];
         const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
@@ -348,15 +460,12 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                    const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                    const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                    const int* __restrict__ b_ci, uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC,
-                   int* __restrict__ tile_cnt, unsigned long long* ticket, int4* __restrict__ cursor_g, int* __restrict__ walk_g,
-                   int max_na) {
+                   int* __restrict__ tile_cnt, unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* masks32 = smem;                      // [16][WS] halfwords
-    int4* cur_s = reinterpret_cast<int4*>(masks32 + WS * 8);
-    int* wstart_s = reinterpret_cast<int*>(cur_s + MAXA_SMEM);
-    int* woff_s = wstart_s + MAXA_SMEM;
-    uint8_t* wrow_s = reinterpret_cast<uint8_t*>(woff_s + MAXA_SMEM);
-    uint32_t* bm = reinterpret_cast<uint32_t*>(wrow_s + MAXA_SMEM);
+    int* cur_s = reinterpret_cast<int*>(masks32 + WS * 8);  // 4 x MAXA_SMEM
+    const SegList sl = seglist_at(cur_s + 4 * MAXA_SMEM);
+    uint32_t* bm = reinterpret_cast<uint32_t*>(sl.row + AL);
     uint32_t* pre = bm + nwords_b;
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
@@ -365,15 +474,9 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
-        const bool in_smem = it.na <= MAXA_SMEM;
-        int4* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
-        WalkBuf wb;
-        if (in_smem) { wb.start = wstart_s; wb.off = woff_s; wb.row = wrow_s; }
-        else {
-            int* g = walk_g + (int64_t)blockIdx.x * max_na * 3;
-            wb.start = g; wb.off = g + max_na; wb.row = reinterpret_cast<uint8_t*>(g + 2 * (int64_t)max_na);
-        }
-        init_cursors(it, cur, colidxC, a_ci, b_rp, b_ci);
+        const Cursors cu = it.na <= MAXA_SMEM ? cursors_at(cur_s, MAXA_SMEM)
+                                              : cursors_at(cursor_g + (int64_t)blockIdx.x * 4 * max_na, max_na);
+        init_cursors(it, cu, colidxC, a_ci, b_rp, b_ci);
         for (int w0 = it.rs; w0 < it.re; w0 += WS) {
             const int nt = min(WS, it.re - w0);
             const int jlo = colidxC[w0], jhi = colidxC[w0 + nt - 1];
@@ -381,7 +484,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, b_ci, wb, s_sh, SymOp{bm, pre, wlo, masks32});
+            walk_window(it, cu, s_rows, limit, b_ci, sl, s_sh, SymOp{bm, pre, wlo, masks32});
             for (int x = tid; x < nt; x += RW_THREADS) {
                 uint32_t mw[8];
                 uint32_t pw[4] = {0u, 0u, 0u, 0u};
@@ -413,24 +516,23 @@ template <typename ACC>
 __device__ __forceinline__ void acc_add(ACC* a, ACC v) { atomicAdd(a, v); }
 
 template <typename V, typename ACC>
-__global__ void __launch_bounds__(RW_THREADS, 2)
+__global__ void __launch_bounds__(RW_THREADS, sizeof(ACC) == 4 ? 2 : 1)
 rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t nitems,
                   const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                   const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
                   const uint8_t* __restrict__ ptrRowC, const int* __restrict__ a_rp, const int* __restrict__ a_ci,
                   const V* __restrict__ a_val, const int* __restrict__ b_rp, const int* __restrict__ b_ci,
                   const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
-                  unsigned long long* ticket, int4* __restrict__ cursor_g, int* __restrict__ walk_g, int max_na) {
+                  unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     ACC* acc = reinterpret_cast<ACC*>(smem);                                   // NW_VALS + 256
     uint16_t* mk = reinterpret_cast<uint16_t*>(acc + NW_VALS + 256);           // [NW_MAXT][16]
     uint8_t* pr = reinterpret_cast<uint8_t*>(mk + NW_MAXT * TS);               // [NW_MAXT][16]
     int* vbase = reinterpret_cast<int*>(pr + NW_MAXT * TS);                    // NW_MAXT
-    int4* cur_s = reinterpret_cast<int4*>(vbase + NW_MAXT);                    // MAXA_SMEM
-    int* wstart_s = reinterpret_cast<int*>(cur_s + MAXA_SMEM);
-    int* woff_s = wstart_s + MAXA_SMEM;
-    uint8_t* wrow_s = reinterpret_cast<uint8_t*>(woff_s + MAXA_SMEM);
-    uint32_t* bm = reinterpret_cast<uint32_t*>(wrow_s + MAXA_SMEM);
+    uint8_t* colb = reinterpret_cast<uint8_t*>(vbase + NW_MAXT);               // NW_VALS + 256
+    int* cur_s = reinterpret_cast<int*>(colb + NW_VALS + 256);                 // 4 x MAXA_SMEM
+    const SegList sl = seglist_at(cur_s + 4 * MAXA_SMEM);
+    uint32_t* bm = reinterpret_cast<uint32_t*>(sl.row + AL);
     uint32_t* pre = bm + nwords_b;
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
@@ -440,15 +542,9 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
-        const bool in_smem = it.na <= MAXA_SMEM;
-        int4* cur = in_smem ? cur_s : (cursor_g + (int64_t)blockIdx.x * max_na);
-        WalkBuf wb;
-        if (in_smem) { wb.start = wstart_s; wb.off = woff_s; wb.row = wrow_s; }
-        else {
-            int* g = walk_g + (int64_t)blockIdx.x * max_na * 3;
-            wb.start = g; wb.off = g + max_na; wb.row = reinterpret_cast<uint8_t*>(g + 2 * (int64_t)max_na);
-        }
-        init_cursors(it, cur, colidxC, a_ci, b_rp, b_ci);
+        const Cursors cu = it.na <= MAXA_SMEM ? cursors_at(cur_s, MAXA_SMEM)
+                                              : cursors_at(cursor_g + (int64_t)blockIdx.x * 4 * max_na, max_na);
+        init_cursors(it, cu, colidxC, a_ci, b_rp, b_ci);
         int t0 = it.rs;
         while (t0 < it.re) {
             // window [t0, t1): at most NW_MAXT tiles and NW_VALS values (a tile holds <= 256)
@@ -482,18 +578,25 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cur, s_rows, limit, b_ci, wb, s_sh,
+            walk_window(it, cu, s_rows, limit, b_ci, sl, s_sh,
                         NumOp<V, ACC>{bm, pre, wlo, mk, pr, vbase, acc, a_val, b_val, it.e0});
-            for (int x = tid; x < nv; x += RW_THREADS) valC[v0 + x] = (V)acc[x];
+            // column bytes of the window into shared memory, then both value and
+            // column arrays leave with coalesced stores
             for (int x = tid; x < ntw * TS; x += RW_THREADS) {
                 const int lt = x >> 4, r = x & 15;
                 uint32_t m16 = mk[lt * TS + r];
-                int64_t p = v0 + vbase[lt] + pr[lt * TS + r];
+                int p = vbase[lt] + pr[lt * TS + r];
                 while (m16) {
                     const int c = __clz(m16) - 16;
-                    colC[p++] = (uint8_t)((r << 4) | c);
+                    colb[p] = (uint8_t)((r << 4) | c);
+                    p++;
                     m16 &= ~(0x8000u >> c);
                 }
+            }
+            __syncthreads();
+            for (int x = tid; x < nv; x += RW_THREADS) {
+                valC[v0 + x] = (V)acc[x];
+                colC[v0 + x] = colb[x];
             }
             __syncthreads();
             t0 = t1;
@@ -502,13 +605,14 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 }
 
 size_t sym_smem(int nwords_b) {
-    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * (16 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
+    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * 16 + SEGLIST_BYTES + 2 * (size_t)nwords_b * 4;
 }
 
 template <typename ACC>
 size_t num_smem(int nwords_b) {
     return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 2 + (size_t)NW_MAXT * TS +
-           (size_t)NW_MAXT * 4 + (size_t)MAXA_SMEM * (16 + 4 + 4 + 1) + 2 * (size_t)nwords_b * 4;
+           (size_t)NW_MAXT * 4 + (size_t)(NW_VALS + 256) + (size_t)MAXA_SMEM * 16 + SEGLIST_BYTES +
+           2 * (size_t)nwords_b * 4;
 }
 
 }  // namespace
@@ -558,12 +662,11 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
     rp->max_na = (int)mx;
     SPG_TRY(spg_read_i64(h, (const int64_t*)(rp->counters + 3), &h->stats.products));
     // cursor scratch for tile-rows with more A nonzeros than fit in shared
-    // memory: one slice per resident CTA (<= 4 CTAs of 512 threads per SM)
+    // memory: one slice of 4 ints per nonzero per resident CTA (<= 4 CTAs of
+    // 512 threads per SM)
     rp->grid = h->num_sms * 4;
-    if (rp->max_na > MAXA_SMEM) {
-        SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na + 1));  // int4 each
-        SPG_TRY(spg_alloc_t(h, &rp->walk_g, (size_t)rp->grid * rp->max_na * 3 + 1));
-    }
+    if (rp->max_na > MAXA_SMEM)
+        SPG_TRY(spg_alloc_t(h, &rp->cursor_g, (size_t)rp->grid * rp->max_na * 4 + 4));
     return SPG_OK;
 }
 
@@ -582,7 +685,7 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
     rw_symbolic_kernel<<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, A->row_ptr,
-        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->walk_g, rp->max_na);
+        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }
@@ -602,8 +705,7 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
     rw_numeric_kernel<V, ACC><<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
-        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->walk_g,
-        rp->max_na);
+        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }
@@ -628,7 +730,6 @@ void rowwise_free_priv(spg_handle_t h, RowwisePriv* rp) {
     spg_free_async(h, rp->item_prefix);
     spg_free_async(h, rp->counters);
     spg_free_async(h, rp->cursor_g);
-    spg_free_async(h, rp->walk_g);
     *rp = RowwisePriv{};
 }
 

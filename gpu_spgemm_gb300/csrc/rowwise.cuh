@@ -8,8 +8,7 @@ struct RowwisePriv {
     int64_t nitems = 0;
     int max_na = 0;                  // largest number of A nonzeros in one tile-row
     unsigned long long* counters = nullptr;  // [0] symbolic ticket, [1] numeric ticket, [2] max nA
-    int4* cursor_g = nullptr;        // per-CTA cursor scratch for tile-rows with many A nonzeros
-    int* walk_g = nullptr;           // per-CTA walk scratch (segment starts, offsets, rows) for the same
+    int* cursor_g = nullptr;         // per-CTA cursor scratch (4 ints per A nonzero) for tile-rows with many A nonzeros
     int grid = 0;
 };
 
