@@ -34,9 +34,7 @@ constexpr int WS = 2048;        // C tiles per symbolic window
 constexpr int NW_MAXT = 768;    // C tiles per numeric window
 constexpr int NW_VALS = 6144;   // C values per numeric window
 constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose cursors fit in shared memory
-constexpr int AL = 1024;        // segments per list of the walk (shared memory)
-constexpr int FU = AL / RW_THREADS;  // A nonzeros per thread per filter step
-constexpr int WCHUNK = 8;       // products per thread per step of the flattened walk (loads in flight)
+constexpr int SWU = 4;          // 32-product steps per sweep round of a warp (loads in flight)
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
     while (lo < hi) {
@@ -176,33 +174,34 @@ __device__ void init_cursors(const ItemInfo& it, Cursors cu, const int* __restri
     __syncthreads();
 }
 
-// Bitmap of a window's (sorted, distinct) tile columns plus per-word popcount
-// prefix: rank(j) = index of column j among the window's tiles.
-__device__ void build_window_rank(const int* __restrict__ colidxC, int t0, int nt, int wlo, int nwd,
-                                  uint32_t* bm, uint32_t* pre, int64_t* s_sh) {
-    for (int x = threadIdx.x; x < nwd; x += RW_THREADS) bm[x] = 0u;
+// Bitmap of a window's (sorted, distinct) tile columns with the popcount
+// prefix of every word beside it (bp[w] = {bits, prefix}, one 8-byte load):
+// rank(j) = index of column j among the window's tiles.
+__device__ void build_window_rank(const int* __restrict__ colidxC, int t0, int nt, int wlo, int nwd, uint2* bp,
+                                  int64_t* s_sh) {
+    for (int x = threadIdx.x; x < nwd; x += RW_THREADS) bp[x] = make_uint2(0u, 0u);
     __syncthreads();
     for (int x = threadIdx.x; x < nt; x += RW_THREADS) {
         const int j = colidxC[t0 + x];
-        atomicOr(&bm[(j >> 5) - wlo], 1u << (j & 31));
+        atomicOr(&bp[(j >> 5) - wlo].x, 1u << (j & 31));
     }
     __syncthreads();
     const int wpt = (nwd + RW_THREADS - 1) / RW_THREADS;
     const int a = min(nwd, (int)threadIdx.x * wpt), b = min(nwd, a + wpt);
     int64_t local = 0;
-    for (int x = a; x < b; x++) local += __popc(bm[x]);
+    for (int x = a; x < b; x++) local += __popc(bp[x].x);
     int64_t tot;
     int64_t run = block_excl_scan<int64_t>(local, s_sh, &tot);
     for (int x = a; x < b; x++) {
-        pre[x] = (uint32_t)run;
-        run += __popc(bm[x]);
+        bp[x].y = (uint32_t)run;
+        run += __popc(bp[x].x);
     }
     __syncthreads();
 }
 
-__device__ __forceinline__ int wrank(const uint32_t* bm, const uint32_t* pre, int wlo, int j) {
-    const int w = (j >> 5) - wlo;
-    return (int)pre[w] + __popc(bm[w] & ((1u << (j & 31)) - 1u));
+__device__ __forceinline__ int wrank(const uint2* bp, int wlo, int j) {
+    const uint2 e = bp[(j >> 5) - wlo];
+    return (int)e.y + __popc(e.x & ((1u << (j & 31)) - 1u));
 }
 
 __device__ __forceinline__ int row_of(const int* s_rows, int e) {
@@ -212,25 +211,7 @@ __device__ __forceinline__ int row_of(const int* s_rows, int e) {
     return r;
 }
 
-// Segment list of the walk, in shared memory: entry k is A nonzero ax[k]
-// (row row[k] of the tile-row) with the B positions [start[k], start[k] +
-// off[k+1] - off[k]) below the window's limit; off[] is the exclusive prefix
-// of the segment lengths, off[K] the list's total.
-struct SegList {
-    int* ax;
-    int* start;
-    int* off;  // AL + 1
-    uint8_t* row;
-};
-
-// ax, start: AL ints each; off: AL + 4 ints (keeps 16-byte alignment); row: AL bytes
-constexpr size_t SEGLIST_BYTES = (size_t)AL * 4 * 3 + 16 + AL;
-
-__device__ __forceinline__ SegList seglist_at(int* base) {
-    return SegList{base, base + AL, base + 2 * AL, reinterpret_cast<uint8_t*>(base + 3 * AL + 4)};
-}
-
-// Segment end of one listed nonzero: the first position >= p0 + 1 whose
+// Segment end of one active nonzero: the first position >= p0 + 1 whose
 // column reaches `limit` (b_ci[p0] < limit is known).  The guess g (the
 // nonzero's previous segment length) is probed first together with its
 // successor, so a repeat of the last length costs one round of loads; a
@@ -267,188 +248,128 @@ __device__ __forceinline__ int segment_end(const int* __restrict__ b_ci, int p0,
     return hi;
 }
 
-// Runs `op` for every B entry of the K listed nonzeros' segments:
-//   1. each listed nonzero's segment end (segment_end), its cursor moved past
-//      the window;
-//   2. a block-wide exclusive scan of the lengths;
-//   3. all threads sweep the flattened products in contiguous chunks of
-//      WCHUNK, one binary search of off[] per chunk to find the owning
-//      segment, then every load of the chunk in flight at once, then the
-//      products: no serial dependency chains and no idle lanes, however
-//      skewed the segment lengths are.
-template <typename Op>
-__device__ __forceinline__ void run_list(const ItemInfo& it, Cursors cu, const int* s_rows, int limit,
-                                         const int* __restrict__ b_ci, SegList sl, int K, int64_t* s_sh, Op op) {
-    const int tid = threadIdx.x;
-    // 1. segment ends: blocked assignment (<= FU entries a thread) so the
-    //    scan below is contiguous; every entry's loads are issued together
-    const int per = (K + RW_THREADS - 1) / RW_THREADS;
-    const int k0 = min(K, tid * per), k1 = min(K, k0 + per);
-    int xs[FU], p0[FU], be[FU], g[FU], pa[FU], pb[FU], ln[FU];
-#pragma unroll
-    for (int u = 0; u < FU; u++) {
-        const int k = k0 + u;
-        xs[u] = k < k1 ? sl.ax[k] : -1;
-        if (xs[u] >= 0) {
-            p0[u] = cu.pos[xs[u]];
-            be[u] = cu.end[xs[u]];
-            g[u] = cu.len[xs[u]];
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < FU; u++) {
-        if (xs[u] >= 0) {
-            g[u] = max(1, min(g[u], be[u] - p0[u]));
-            pa[u] = g[u] > 1 ? __ldg(&b_ci[p0[u] + g[u] - 1]) : INT_MIN;
-            pb[u] = p0[u] + g[u] < be[u] ? __ldg(&b_ci[p0[u] + g[u]]) : INT_MAX;
-        }
-    }
-    int local = 0;
-#pragma unroll 1
-    for (int u = 0; u < FU; u++) {
-        ln[u] = 0;
-        if (xs[u] >= 0) {
-            int nc;
-            const int hi = segment_end(b_ci, p0[u], be[u], g[u], pa[u], pb[u], limit, &nc);
-            ln[u] = hi - p0[u];
-            cu.pos[xs[u]] = hi;
-            cu.col[xs[u]] = nc;
-            cu.len[xs[u]] = ln[u];
-            sl.start[k0 + u] = p0[u];
-            sl.row[k0 + u] = (uint8_t)row_of(s_rows, it.e0 + xs[u]);
-            local += ln[u];
-        }
-    }
-    // 2. exclusive scan of the lengths
-    int64_t total;
-    int run = (int)block_excl_scan<int64_t>(local, s_sh, &total);
-#pragma unroll
-    for (int u = 0; u < FU; u++)
-        if (xs[u] >= 0) {
-            sl.off[k0 + u] = run;
-            run += ln[u];
-        }
-    const int P = (int)total;
-    if (tid == 0) sl.off[K] = P;
-    __syncthreads();
-    // 3. flattened products in contiguous chunks of WCHUNK: positions first,
-    //    then every load of the chunk in flight at once, then the products
-    for (int q0 = tid * WCHUNK; q0 < P; q0 += RW_THREADS * WCHUNK) {
-        int lo = 0, hi = K;  // last k with off[k] <= q0
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (sl.off[mid] <= q0) lo = mid; else hi = mid;
-        }
-        int k = lo;
-        int next = sl.off[k + 1];
-        int pk[WCHUNK], pp[WCHUNK];
-#pragma unroll
-        for (int u = 0; u < WCHUNK; u++) {
-            const int q = q0 + u;
-            if (q < P) {
-                while (q >= next) {  // every segment is non-empty: at most WCHUNK steps
-                    k++;
-                    next = sl.off[k + 1];
-                }
-                pk[u] = k;
-                pp[u] = sl.start[k] + (q - sl.off[k]);
-            } else {
-                pk[u] = -1;
-                pp[u] = 0;
-            }
-        }
-        typename Op::Loaded ld[WCHUNK];
-        int cc[WCHUNK];
-#pragma unroll
-        for (int u = 0; u < WCHUNK; u++) {
-            cc[u] = pk[u] >= 0 ? __ldg(&b_ci[pp[u]]) : 0;
-            ld[u] = op.load(pk[u] >= 0 ? sl.ax[pk[u]] : -1, pp[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < WCHUNK; u++)
-            if (pk[u] >= 0) op.apply(sl.row[pk[u]], cc[u], ld[u]);
-    }
-    __syncthreads();
-}
-
-// Runs `op(r, c, loaded)` for every B entry (column c < limit) that the A
-// nonzeros of the tile-row reach inside the current window, and moves each
-// nonzero's cursor past the window.  A filter pass reads only the cursor
-// columns (coalesced, FU per thread) and lists the nonzeros with an entry
-// below the limit; a full list of AL entries (or the last one) goes through
-// run_list.  Nonzeros with nothing in the window cost one 4-byte load.
+// Runs the products of every B entry (column c < limit) that the A nonzeros
+// of the tile-row reach inside the current window, and moves each nonzero's
+// cursor past the window.  Warp-centric, with no block-wide barrier inside:
+// a warp takes the next 32 nonzeros from the block's counter *s_fx (zeroed
+// by the caller), each lane finds the window segment of its own nonzero
+// (segment_end, from the cursor), a shuffle scan flattens the warp's
+// segments, and the warp sweeps the products lane by lane, SWU steps of 32
+// per round with all their loads in flight: consecutive lanes read
+// consecutive B entries of one segment, and a slow search stalls only its
+// own warp.  The caller synchronises the block afterwards.
 template <typename Op>
 __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, const int* s_rows, int limit,
-                                            const int* __restrict__ b_ci, SegList sl, int64_t* s_sh, Op op) {
-    const int tid = threadIdx.x;
-    int K = 0;  // listed entries (block-uniform)
-    for (int f0 = 0; f0 < it.na; f0 += AL) {
-        int fx[FU];
-        int cnt = 0;
-#pragma unroll
-        for (int u = 0; u < FU; u++) {
-            const int x = f0 + u * RW_THREADS + tid;
-            fx[u] = (x < it.na && cu.col[x] < limit) ? x : -1;
-            cnt += fx[u] >= 0 ? 1 : 0;
+                                            const int* __restrict__ b_ci, int* s_fx, Op op) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(s_fx, 32);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= it.na) break;
+        const int x = base + lane;
+        int len = 0, p0 = 0, r = 0;
+        typename Op::Entry ent{};
+        if (x < it.na && cu.col[x] < limit) {
+            p0 = cu.pos[x];
+            const int be = cu.end[x];
+            const int g = max(1, min(cu.len[x], be - p0));
+            const int pa = g > 1 ? __ldg(&b_ci[p0 + g - 1]) : INT_MIN;
+            const int pb = p0 + g < be ? __ldg(&b_ci[p0 + g]) : INT_MAX;
+            ent = op.entry(x);
+            r = row_of(s_rows, it.e0 + x);
+            int nc;
+            const int hi = segment_end(b_ci, p0, be, g, pa, pb, limit, &nc);
+            len = hi - p0;
+            cu.pos[x] = hi;
+            cu.col[x] = nc;
+            cu.len[x] = len;
         }
-        int64_t tot;
-        int k = (int)block_excl_scan<int64_t>(cnt, s_sh, &tot);
-        if (K + (int)tot > AL) {
-            run_list(it, cu, s_rows, limit, b_ci, sl, K, s_sh, op);
-            K = 0;
-        }
-        k += K;
+        int inc = len;
 #pragma unroll
-        for (int u = 0; u < FU; u++)
-            if (fx[u] >= 0) sl.ax[k++] = fx[u];
-        K += (int)tot;
-    }
-    if (K > 0) {
-        __syncthreads();
-        run_list(it, cu, s_rows, limit, b_ci, sl, K, s_sh, op);
+        for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(FULL, inc, d);
+            if (lane >= d) inc += o;
+        }
+        const int P = __shfl_sync(FULL, inc, 31);
+        const int off = inc - len;  // exclusive offset of this lane's segment
+        for (int q0 = 0; q0 < P; q0 += 32 * SWU) {
+            int pp[SWU], rr[SWU];
+            typename Op::Entry ee[SWU];
+#pragma unroll
+            for (int u = 0; u < SWU; u++) {
+                const int q = q0 + u * 32 + lane;
+                // owner: last lane j with off_j <= q (it has q < off_j + len_j)
+                int lo = 0, hi = 32;
+#pragma unroll
+                for (int s2 = 0; s2 < 5; s2++) {
+                    const int mid = (lo + hi) >> 1;
+                    const int om = __shfl_sync(FULL, off, mid);
+                    if (om <= q) lo = mid; else hi = mid;
+                }
+                const int jp0 = __shfl_sync(FULL, p0, lo), joff = __shfl_sync(FULL, off, lo);
+                rr[u] = __shfl_sync(FULL, r, lo);
+                ee[u] = op.shfl(ent, lo);
+                pp[u] = q < P ? jp0 + (q - joff) : -1;
+            }
+            typename Op::Loaded ld[SWU];
+            int cc[SWU];
+#pragma unroll
+            for (int u = 0; u < SWU; u++) {
+                cc[u] = pp[u] >= 0 ? __ldg(&b_ci[pp[u]]) : 0;
+                ld[u] = op.load(pp[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < SWU; u++)
+                if (pp[u] >= 0) op.apply(rr[u], cc[u], ee[u], ld[u]);
+        }
     }
 }
+
+// The walk's operations: entry(x) once per active nonzero (passed between
+// lanes by shfl), load(p) per product with the round's other loads, and
+// apply(r, c, entry, loaded).
 
 // Symbolic product: OR the column's bit into C's row mask.
 struct SymOp {
+    struct Entry {};
     struct Loaded {};
-    const uint32_t* bm;
-    const uint32_t* pre;
+    const uint2* bp;
     int wlo;
     uint32_t* masks32;
-    __device__ __forceinline__ Loaded load(int, int) const { return Loaded{}; }
-    __device__ __forceinline__ void apply(int r, int c, Loaded) const {
-        const int lt = wrank(bm, pre, wlo, c >> 4);
-        const int idx = r * WS + lt;
+    __device__ __forceinline__ Entry entry(int) const { return Entry{}; }
+    __device__ __forceinline__ Entry shfl(Entry, int) const { return Entry{}; }
+    __device__ __forceinline__ Loaded load(int) const { return Loaded{}; }
+    __device__ __forceinline__ void apply(int r, int c, Entry, Loaded) const {
+        const int idx = r * WS + wrank(bp, wlo, c >> 4);
         atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
     }
 };
 
-// Numeric product: a_ik * b_kc into C's value slot.
+// Numeric product: a_ik * b_kc into C's value slot.  A window's C tile rows
+// are one word each, (value offset of the row << 16) | row mask.
 template <typename V, typename ACC>
 struct NumOp {
-    struct Loaded { ACC va, vb; };
-    const uint32_t* bm;
-    const uint32_t* pre;
+    struct Entry { ACC va; };
+    struct Loaded { ACC vb; };
+    const uint2* bp;
     int wlo;
-    const uint16_t* mk;
-    const uint8_t* pr;
-    const int* vbase;
+    const uint32_t* words;
     ACC* acc;
     const V* a_val;
     const V* b_val;
     int e0;
-    __device__ __forceinline__ Loaded load(int x, int p) const {
-        Loaded l;
-        l.va = x >= 0 ? (ACC)__ldg(&a_val[e0 + x]) : ACC(0);
-        l.vb = x >= 0 ? (ACC)__ldg(&b_val[p]) : ACC(0);
-        return l;
+    __device__ __forceinline__ Entry entry(int x) const { return Entry{(ACC)__ldg(&a_val[e0 + x])}; }
+    __device__ __forceinline__ Entry shfl(Entry e, int src) const {
+        return Entry{__shfl_sync(0xffffffffu, e.va, src)};
     }
-    __device__ __forceinline__ void apply(int r, int c, Loaded l) const {
-        const int lt = wrank(bm, pre, wlo, c >> 4);
-        const uint32_t m16 = mk[lt * TS + r];
-        const int pos = vbase[lt] + pr[lt * TS + r] + __popc(m16 >> (16 - (c & 15)));
-        atomicAdd(&acc[pos], l.va * l.vb);
+    __device__ __forceinline__ Loaded load(int p) const {
+        return Loaded{p >= 0 ? (ACC)__ldg(&b_val[p]) : ACC(0)};
+    }
+    __device__ __forceinline__ void apply(int r, int c, Entry e, Loaded l) const {
+        const uint32_t w = words[wrank(bp, wlo, c >> 4) * TS + r];
+        atomicAdd(&acc[(int)(w >> 16) + __popc((w & 0xffffu) >> (16 - (c & 15)))], e.va * l.vb);
     }
 };
 
@@ -464,12 +385,11 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* masks32 = smem;                      // [16][WS] halfwords
     int* cur_s = reinterpret_cast<int*>(masks32 + WS * 8);  // 4 x MAXA_SMEM
-    const SegList sl = seglist_at(cur_s + 4 * MAXA_SMEM);
-    uint32_t* bm = reinterpret_cast<uint32_t*>(sl.row + AL);
-    uint32_t* pre = bm + nwords_b;
+    uint2* bp = reinterpret_cast<uint2*>(cur_s + 4 * MAXA_SMEM);  // nwords_b
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
+    __shared__ int s_fx;
     const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
@@ -483,8 +403,10 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
-            build_window_rank(colidxC, w0, nt, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cu, s_rows, limit, b_ci, sl, s_sh, SymOp{bm, pre, wlo, masks32});
+            if (tid == 0) s_fx = 0;
+            build_window_rank(colidxC, w0, nt, wlo, nwd, bp, s_sh);
+            walk_window(it, cu, s_rows, limit, b_ci, &s_fx, SymOp{bp, wlo, masks32});
+            __syncthreads();
             for (int x = tid; x < nt; x += RW_THREADS) {
                 uint32_t mw[8];
                 uint32_t pw[4] = {0u, 0u, 0u, 0u};
@@ -526,18 +448,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     ACC* acc = reinterpret_cast<ACC*>(smem);                                   // NW_VALS + 256
-    uint16_t* mk = reinterpret_cast<uint16_t*>(acc + NW_VALS + 256);           // [NW_MAXT][16]
-    uint8_t* pr = reinterpret_cast<uint8_t*>(mk + NW_MAXT * TS);               // [NW_MAXT][16]
-    int* vbase = reinterpret_cast<int*>(pr + NW_MAXT * TS);                    // NW_MAXT
-    uint8_t* colb = reinterpret_cast<uint8_t*>(vbase + NW_MAXT);               // NW_VALS + 256
-    int* cur_s = reinterpret_cast<int*>(colb + NW_VALS + 256);                 // 4 x MAXA_SMEM
-    const SegList sl = seglist_at(cur_s + 4 * MAXA_SMEM);
-    uint32_t* bm = reinterpret_cast<uint32_t*>(sl.row + AL);
-    uint32_t* pre = bm + nwords_b;
+    uint32_t* words = reinterpret_cast<uint32_t*>(acc + NW_VALS + 256);        // [NW_MAXT][16]
+    int* cur_s = reinterpret_cast<int*>(words + NW_MAXT * TS);                 // 4 x MAXA_SMEM
+    uint2* bp = reinterpret_cast<uint2*>(cur_s + 4 * MAXA_SMEM);               // nwords_b
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
-    __shared__ int s_nt;
+    __shared__ int s_nt, s_fx;
     const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
@@ -568,36 +485,31 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             const int jlo = colidxC[t0], jhi = colidxC[t1 - 1];
             const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
             const int limit = (jhi + 1) * TS;
-            for (int x = tid; x < ntw; x += RW_THREADS) {
-                const int64_t t = (int64_t)t0 + x;
-                vbase[x] = (int)(tile_nnzC[t] - v0);
-                const uint4* mi = reinterpret_cast<const uint4*>(maskC) + 2 * t;
-                reinterpret_cast<uint4*>(mk)[2 * x] = mi[0];
-                reinterpret_cast<uint4*>(mk)[2 * x + 1] = mi[1];
-                reinterpret_cast<uint4*>(pr)[x] = reinterpret_cast<const uint4*>(ptrRowC)[t];
+            for (int x = tid; x < ntw * TS; x += RW_THREADS) {
+                const int64_t t = (int64_t)t0 + (x >> 4);
+                const uint32_t base = (uint32_t)(tile_nnzC[t] - v0) + ptrRowC[(int64_t)t0 * TS + x];
+                words[x] = (base << 16) | maskC[(int64_t)t0 * TS + x];
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
-            build_window_rank(colidxC, t0, ntw, wlo, nwd, bm, pre, s_sh);
-            walk_window(it, cu, s_rows, limit, b_ci, sl, s_sh,
-                        NumOp<V, ACC>{bm, pre, wlo, mk, pr, vbase, acc, a_val, b_val, it.e0});
-            // column bytes of the window into shared memory, then both value and
-            // column arrays leave with coalesced stores
+            if (tid == 0) s_fx = 0;
+            build_window_rank(colidxC, t0, ntw, wlo, nwd, bp, s_sh);
+            walk_window(it, cu, s_rows, limit, b_ci, &s_fx,
+                        NumOp<V, ACC>{bp, wlo, words, acc, a_val, b_val, it.e0});
+            __syncthreads();
+            // column bytes: one thread per C tile row writes its run (runs of
+            // consecutive rows are adjacent in colC); values leave coalesced
             for (int x = tid; x < ntw * TS; x += RW_THREADS) {
-                const int lt = x >> 4, r = x & 15;
-                uint32_t m16 = mk[lt * TS + r];
-                int p = vbase[lt] + pr[lt * TS + r];
+                const uint32_t w = words[x];
+                uint32_t m16 = w & 0xffffu;
+                uint8_t* o = colC + v0 + (w >> 16);
+                const uint8_t rb = (uint8_t)((x & 15) << 4);
                 while (m16) {
                     const int c = __clz(m16) - 16;
-                    colb[p] = (uint8_t)((r << 4) | c);
-                    p++;
+                    *o++ = rb | (uint8_t)c;
                     m16 &= ~(0x8000u >> c);
                 }
             }
-            __syncthreads();
-            for (int x = tid; x < nv; x += RW_THREADS) {
-                valC[v0 + x] = (V)acc[x];
-                colC[v0 + x] = colb[x];
-            }
+            for (int x = tid; x < nv; x += RW_THREADS) valC[v0 + x] = (V)acc[x];
             __syncthreads();
             t0 = t1;
         }
@@ -605,14 +517,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 }
 
 size_t sym_smem(int nwords_b) {
-    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * 16 + SEGLIST_BYTES + 2 * (size_t)nwords_b * 4;
+    return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * 16 + (size_t)nwords_b * 8;
 }
 
 template <typename ACC>
 size_t num_smem(int nwords_b) {
-    return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 2 + (size_t)NW_MAXT * TS +
-           (size_t)NW_MAXT * 4 + (size_t)(NW_VALS + 256) + (size_t)MAXA_SMEM * 16 + SEGLIST_BYTES +
-           2 * (size_t)nwords_b * 4;
+    return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 4 + (size_t)MAXA_SMEM * 16 +
+           (size_t)nwords_b * 8;
 }
 
 }  // namespace
