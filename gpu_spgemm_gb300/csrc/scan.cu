@@ -89,9 +89,79 @@ scan_lookback_kernel(const Tin* in, Tout* out, int64_t n, unsigned long long* st
     }
 }
 
+// Long scans (C's 1.8e9 tile counts on a power-law product) run as two
+// streaming passes instead: per-warp sums of 1024-item slices, a (short)
+// look-back scan of those sums, then every warp rescans its slice with
+// shuffles from its offset.  No block waits on another, all accesses are
+// coalesced, and the traffic is two reads and one write of the array.
+constexpr int WS_THREADS = 256;
+constexpr int WS_SLICE = 1024;  // items per warp
+constexpr int WS_TILE = WS_SLICE * (WS_THREADS / 32);
+constexpr int64_t WS_MIN_N = 1 << 22;
+
+template <typename Tin>
+__global__ void __launch_bounds__(WS_THREADS)
+slice_sum_kernel(const Tin* __restrict__ in, int64_t n, int64_t nslices, int64_t* __restrict__ sums) {
+    const int lane = threadIdx.x & 31;
+    const int64_t sl = (int64_t)blockIdx.x * (WS_THREADS / 32) + (threadIdx.x >> 5);
+    if (sl >= nslices) return;
+    const int64_t b = sl * WS_SLICE;
+    int64_t v = 0;
+#pragma unroll 8
+    for (int k = 0; k < WS_SLICE / 32; k++) {
+        const int64_t idx = b + k * 32 + lane;
+        if (idx < n) v += (int64_t)in[idx];
+    }
+    v = warp_sum(v);
+    if (lane == 0) sums[sl] = v;
+}
+
+template <typename Tin, typename Tout>
+__global__ void __launch_bounds__(WS_THREADS)
+slice_scan_kernel(const Tin* in, Tout* out, int64_t n, int64_t nslices, const int64_t* __restrict__ offs) {
+    const int lane = threadIdx.x & 31;
+    const int64_t sl = (int64_t)blockIdx.x * (WS_THREADS / 32) + (threadIdx.x >> 5);
+    if (sl >= nslices) return;
+    const int64_t b = sl * WS_SLICE;
+    int64_t carry = offs[sl];
+#pragma unroll 4
+    for (int k = 0; k < WS_SLICE / 32; k++) {
+        const int64_t idx = b + k * 32 + lane;
+        const int64_t v = idx < n ? (int64_t)in[idx] : 0;
+        int64_t inc = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int64_t o = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= d) inc += o;
+        }
+        if (idx <= n) out[idx] = (Tout)(carry + inc - v);
+        carry += __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+template <typename Tin, typename Tout>
+spg_status scan_impl(spg_handle_t h, const Tin* in, Tout* out, int64_t n);
+
+template <typename Tin, typename Tout>
+spg_status scan_long(spg_handle_t h, const Tin* in, Tout* out, int64_t n) {
+    const int64_t nslices = ceil_div(n + 1, WS_SLICE);
+    const int64_t nblocks = ceil_div(nslices, WS_THREADS / 32);
+    if (nblocks > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "scan: too long");
+    int64_t* sums = nullptr;
+    SPG_TRY(spg_alloc_t(h, &sums, (size_t)nslices + 1));
+    slice_sum_kernel<Tin><<<(unsigned)nblocks, WS_THREADS, 0, h->stream>>>(in, n, nslices, sums);
+    SPG_CUDA(h, cudaGetLastError());
+    SPG_TRY((scan_impl<int64_t, int64_t>(h, sums, sums, nslices)));
+    slice_scan_kernel<Tin, Tout><<<(unsigned)nblocks, WS_THREADS, 0, h->stream>>>(in, out, n, nslices, sums);
+    SPG_CUDA(h, cudaGetLastError());
+    spg_free_async(h, sums);
+    return SPG_OK;
+}
+
 template <typename Tin, typename Tout>
 spg_status scan_impl(spg_handle_t h, const Tin* in, Tout* out, int64_t n) {
     if (n < 0) return spg_fail(h, SPG_ERR_INVALID, "scan: negative length");
+    if (n >= WS_MIN_N) return scan_long<Tin, Tout>(h, in, out, n);
     const int64_t nblocks = ceil_div(n + 1, SCAN_TILE);
     if (nblocks > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "scan: too long");
     unsigned long long* state = nullptr;

@@ -175,3 +175,18 @@ def test_mixed_precision_tensor_path(handle, name, a):
     st = handle.stats()
     if name in ("stencil27_8", "dense_tile"):
         assert st["tensor_pairs"] > 0
+
+
+def test_long_tile_scan_is_exact(handle):
+    """C with more than 2^22 tiles takes the two-pass streaming scan for
+    tile_nnzC: every prefix step must equal the popcount of its tile's mask."""
+    a = synth.rmat(16, 16)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    C = api.symbolic(handle, A, B, algo="rowwise")
+    assert C.numtileC >= (1 << 22)
+    got = C.to_host(values=False)
+    pc = np.unpackbits(got["maskC"].view(np.uint8)).reshape(-1, 256).sum(1, dtype=np.int64)
+    assert got["tile_nnzC"][0] == 0
+    np.testing.assert_array_equal(np.diff(got["tile_nnzC"]), pc)
+    assert got["tile_nnzC"][-1] == got["nnzC"]
