@@ -251,8 +251,8 @@ __device__ __forceinline__ int segment_end(const int* __restrict__ b_ci, int p0,
 // Runs the products of every B entry (column c < limit) that the A nonzeros
 // of the tile-row reach inside the current window, and moves each nonzero's
 // cursor past the window.  Warp-centric, with no block-wide barrier inside:
-// a warp takes the next 32 nonzeros from the block's counter *s_fx (zeroed
-// by the caller), each lane finds the window segment of its own nonzero
+// a warp takes the next (up to) 32 nonzeros from the block's counter *s_fx
+// (zeroed by the caller), each lane finds the window segment of its own nonzero
 // (segment_end, from the cursor), a shuffle scan flattens the warp's
 // segments, and the warp sweeps the products lane by lane, SWU steps of 32
 // per round with all their loads in flight: consecutive lanes read
@@ -264,14 +264,22 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(s_fx, 32);
+        // guided schedule: a step takes 1/RW_WARPS of what is left (at most
+        // 32), so a short tile-row still spreads over every warp and the
+        // window ends on small steps
+        int base = 0, cnt = 0;
+        if (lane == 0) {
+            const int left = it.na - *reinterpret_cast<volatile int*>(s_fx);
+            cnt = min(32, max(1, (left + RW_WARPS - 1) / RW_WARPS));
+            base = atomicAdd(s_fx, cnt);
+        }
         base = __shfl_sync(FULL, base, 0);
+        cnt = __shfl_sync(FULL, cnt, 0);
         if (base >= it.na) break;
         const int x = base + lane;
         int len = 0, p0 = 0, r = 0;
         typename Op::Entry ent{};
-        if (x < it.na && cu.col[x] < limit) {
+        if (lane < cnt && x < it.na && cu.col[x] < limit) {
             p0 = cu.pos[x];
             const int be = cu.end[x];
             const int g = max(1, min(cu.len[x], be - p0));
