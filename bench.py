@@ -302,8 +302,8 @@ def run_ours(args):
                         "model": os.path.relpath(api.SIZING_MODEL_PATH, ROOT), "margin": args.sizing_margin,
                         "predicted_tiles": stats[-1].get("predicted_tiles", 0), "actual_tiles": numtileC,
                         "overflow_reruns": stats[-1].get("overflow_reruns", 0),
-                        "step1": "one fused count+fill pass" if stats[-1].get("overflow_reruns", 0) == 0
-                        else "fused pass + exact fill re-run"},
+                        "step1": "one bitmap pass into predicted per-row slots, then compaction; "
+                                 "rows that outgrow their slot re-run the exact fill"},
                     "accuracy": accuracy})
         line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,

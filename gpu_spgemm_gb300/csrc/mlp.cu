@@ -226,20 +226,12 @@ __global__ void mlp_adam_kernel(float* __restrict__ p, float* __restrict__ g, fl
 }
 
 // predicted counts -> per-tile-row capacity, summed
-__global__ void mlp_capacity_kernel(int tilem, const float* __restrict__ pred, float margin,
-                                    unsigned long long* __restrict__ cap_tiles, unsigned long long* __restrict__ cap_nnz) {
-    unsigned long long ct = 0, cn = 0;
+// Slot size of each tile-row: the predicted C tile count (the network's
+// target is log1p of it) grown by the margin, plus 2.
+__global__ void mlp_slot_kernel(int tilem, const float* __restrict__ pred, float margin, int* __restrict__ slot) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
         const float t = fmaxf(expm1f(fmaxf(pred[(int64_t)i * NO + 0], 0.f)), 0.f);
-        const float z = fmaxf(expm1f(fmaxf(pred[(int64_t)i * NO + 1], 0.f)), 0.f);
-        ct += (unsigned long long)ceilf(t * (1.f + margin) + 2.f);
-        cn += (unsigned long long)ceilf(z * (1.f + margin) + 16.f);
-    }
-    ct = warp_sum(ct);
-    cn = warp_sum(cn);
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(cap_tiles, ct);
-        atomicAdd(cap_nnz, cn);
+        slot[i] = (int)fminf(ceilf(t * (1.f + margin) + 2.f), 1.0e9f);
     }
 }
 
@@ -398,28 +390,19 @@ extern "C" spg_status spg_set_sizing_model(spg_handle_t h, spg_mlp_t mm, float m
 }
 
 // Predicted capacities for C of A*B (tiles, nonzeros) from the sizing model.
-spg_status mlp_predict_capacity(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int64_t* cap_tiles,
-                                int64_t* cap_nnz) {
+spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz) {
     spg_mlp_t mm = h->sizing;
     const int tilem = A->tilem;
     float *feat = nullptr, *pred = nullptr;
-    unsigned long long* cap = nullptr;
     SPG_TRY(spg_alloc_t(h, &feat, (size_t)tilem * NF + 1));
     SPG_TRY(spg_alloc_t(h, &pred, (size_t)tilem * NO + 1));
-    SPG_TRY(spg_alloc_t(h, &cap, 2));
-    SPG_CUDA(h, cudaMemsetAsync(cap, 0, 16, h->stream));
     SPG_TRY(spg_mlp_features(h, A, B, feat));
     SPG_TRY(spg_mlp_forward(h, mm, feat, tilem, pred));
     if (tilem > 0) {
-        mlp_capacity_kernel<<<mgrid(h, tilem, 256), 256, 0, h->stream>>>(tilem, pred, h->sizing_margin, cap, cap + 1);
+        mlp_slot_kernel<<<mgrid(h, tilem, 256), 256, 0, h->stream>>>(tilem, pred, h->sizing_margin, slot_sz);
         SPG_CUDA(h, cudaGetLastError());
     }
-    SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 16, cap, 16, cudaMemcpyDeviceToHost, h->stream));
-    SPG_CUDA(h, cudaStreamSynchronize(h->stream));
-    *cap_tiles = h->h_pinned[16];
-    *cap_nnz = h->h_pinned[17];
     spg_free_async(h, feat);
     spg_free_async(h, pred);
-    spg_free_async(h, cap);
     return SPG_OK;
 }

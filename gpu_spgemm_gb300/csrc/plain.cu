@@ -97,11 +97,12 @@ c1_count_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict_
 __global__ void __launch_bounds__(C1_THREADS)
 c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
                const int* __restrict__ b_tp, const int* __restrict__ b_tc,
-               const int* __restrict__ tile_ptrC, int* __restrict__ rowidxC, int* __restrict__ colidxC) {
+               const int* __restrict__ tile_ptrC, int* __restrict__ rowidxC, int* __restrict__ colidxC,
+               const int* __restrict__ rows) {
     extern __shared__ uint32_t bm[];
     __shared__ int64_t s_sh[C1_WARPS + 1];
     __shared__ int s_span[4];
-    const int i = blockIdx.x;
+    const int i = rows ? rows[blockIdx.x] : (int)blockIdx.x;
     (void)nwords;
     if (tile_ptrC[i] == tile_ptrC[i + 1]) return;
     build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
@@ -125,101 +126,77 @@ c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__
     }
 }
 
-// Step 1 in ONE pass when C's tile arrays were pre-sized (learned sizing):
-// tile-rows are taken in ticket order by a persistent grid; each builds its
-// bitmap once, publishes its count, gets its output offset by a decoupled
-// look-back over the preceding tile-rows (bounded spin), writes tile_ptrC[i],
-// and fills its tile indices straight from the same bitmap when they fit in
-// the capacity.  If they do not, DERR_OVERFLOW is raised; tile_ptrC is still
-// exact, so the host re-runs only the fill into exactly sized arrays.
+// Step 1 with learned sizing: every tile-row i owns a slot of predicted size
+// in a staging array (slot_off = exclusive scan of the predicted sizes).  One
+// block per tile-row builds its bitmap once, records the exact count, and
+// writes its tile columns into its slot when they fit.  No block waits on
+// another.  Rows that outgrow their slot only keep their count and rebuild
+// their bitmap in the exact fill afterwards (c1_fill_kernel on a row list).
 __global__ void __launch_bounds__(C1_THREADS)
-c1_fused_kernel(int tilem, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
-                const int* __restrict__ b_tp, const int* __restrict__ b_tc, int* __restrict__ tile_ptrC,
-                int* __restrict__ rowidxC, int* __restrict__ colidxC, int64_t cap, int64_t* __restrict__ row_pairs,
-                unsigned long long* __restrict__ pairs_total, unsigned long long* __restrict__ state,
-                unsigned* __restrict__ ticket, unsigned* flags) {
+c1_slot_kernel(const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ b_tp,
+               const int* __restrict__ b_tc, const int64_t* __restrict__ slot_off, int* __restrict__ slot_col,
+               int* __restrict__ cnt, int64_t* __restrict__ row_pairs, unsigned long long* __restrict__ pairs_total) {
     extern __shared__ uint32_t bm[];
-    __shared__ int s_i;
     __shared__ int s_span[4];
     __shared__ int64_t s_sh[C1_WARPS + 1];
-    __shared__ int64_t s_prefix;
     __shared__ int s_c[C1_WARPS];
     __shared__ int64_t s_p[C1_WARPS];
-    const unsigned long long F_AGG = 1ull << 62, F_PRE = 2ull << 62, VM = (1ull << 62) - 1;
+    const int i = blockIdx.x;
+    if (a_tp[i] == a_tp[i + 1]) {
+        if (threadIdx.x == 0) { cnt[i] = 0; row_pairs[i] = 0; }
+        return;
+    }
+    int64_t pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
+    const int wlo = s_span[2], nwd = s_span[3];
+    const int wpt = (nwd + C1_THREADS - 1) / C1_THREADS;
+    const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
+    int64_t local = 0;
+    for (int w = w0; w < w1; w++) local += __popc(bm[w]);
+    int64_t tot;
+    const int64_t run = block_excl_scan<int64_t>(local, s_sh, &tot);
+    pairs = warp_sum(pairs);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    while (true) {
-        if (threadIdx.x == 0) s_i = (int)atomicAdd(ticket, 1u);
-        __syncthreads();
-        const int i = s_i;
-        if (i >= tilem) break;
-        const bool nonempty = a_tp[i] < a_tp[i + 1];
-        int nwd = 0;
-        int64_t pairs = 0;
-        int c = 0;
-        if (nonempty) {
-            pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
-            nwd = s_span[3];
-            for (int w = threadIdx.x; w < nwd; w += C1_THREADS) c += __popc(bm[w]);
-            c = warp_sum(c);
-            pairs = warp_sum(pairs);
-            if (lane == 0) { s_c[warp] = c; s_p[warp] = pairs; }
-            __syncthreads();
-            c = 0;
-            pairs = 0;
-            for (int w = 0; w < C1_WARPS; w++) { c += s_c[w]; pairs += s_p[w]; }
+    if (lane == 0) s_p[warp] = pairs;
+    (void)s_c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t p = 0;
+        for (int w = 0; w < C1_WARPS; w++) p += s_p[w];
+        cnt[i] = (int)tot;
+        row_pairs[i] = p;
+        if (p) atomicAdd(pairs_total, (unsigned long long)p);
+    }
+    if (tot > slot_off[i + 1] - slot_off[i]) return;  // outgrew its slot: exact fill later
+    int64_t pos = slot_off[i] + run;
+    for (int w = w0; w < w1; w++) {
+        uint32_t bits = bm[w];
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            slot_col[pos++] = (wlo + w) * 32 + b;
+            bits &= bits - 1u;
         }
-        if (threadIdx.x == 0) {
-            int64_t prefix = 0;
-            if (i == 0) {
-                atomicExch(&state[0], F_PRE | ((unsigned long long)c & VM));
-            } else {
-                atomicExch(&state[i], F_AGG | ((unsigned long long)c & VM));
-                int j = i - 1, spins = 0;
-                while (j >= 0) {
-                    unsigned long long st;
-                    asm volatile("ld.volatile.global.u64 %0, [%1];" : "=l"(st) : "l"(state + j));
-                    const unsigned long long f = st & ~VM;
-                    if (f == 0) {
-                        if (++spins > SPG_SPIN_LIMIT) { atomicOr(flags, DERR_TIMEOUT); break; }
-                        continue;
-                    }
-                    prefix += (int64_t)(st & VM);
-                    if (f == F_PRE) break;
-                    j--;
-                }
-                __threadfence();
-                atomicExch(&state[i], F_PRE | ((unsigned long long)(prefix + c) & VM));
-            }
-            if (prefix + c > 0x7fffffffLL) atomicOr(flags, DERR_TOO_BIG);
-            tile_ptrC[i] = (int)prefix;
-            if (i == tilem - 1) tile_ptrC[tilem] = (int)(prefix + c);
-            row_pairs[i] = pairs;
-            if (pairs) atomicAdd(pairs_total, (unsigned long long)pairs);
-            if (c > 0 && prefix + c > cap) atomicOr(flags, DERR_OVERFLOW);
-            s_prefix = prefix;
+    }
+}
+
+// Slots -> C's exact tile arrays, one warp per tile-row (coalesced copies);
+// rows that outgrew their slot are listed for the exact fill.
+__global__ void c1_compact_kernel(int tilem, const int* __restrict__ tile_ptrC, const int64_t* __restrict__ slot_off,
+                                  const int* __restrict__ slot_col, int* __restrict__ rowidxC, int* __restrict__ colidxC,
+                                  int* __restrict__ over_rows, unsigned* __restrict__ n_over) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < tilem; i += nw) {
+        const int t0 = tile_ptrC[i], n = tile_ptrC[i + 1] - t0;
+        if (n == 0) continue;
+        const int64_t s0 = slot_off[i];
+        if (n > slot_off[i + 1] - s0) {
+            if (lane == 0) over_rows[atomicAdd(n_over, 1u)] = i;
+            continue;
         }
-        __syncthreads();
-        const int64_t prefix = s_prefix;
-        if (c > 0 && prefix + c <= cap) {
-            const int wlo = s_span[2];
-            const int wpt = (nwd + C1_THREADS - 1) / C1_THREADS;
-            const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
-            int64_t local = 0;
-            for (int w = w0; w < w1; w++) local += __popc(bm[w]);
-            int64_t tot;
-            int64_t pos = prefix + block_excl_scan<int64_t>(local, s_sh, &tot);
-            for (int w = w0; w < w1; w++) {
-                uint32_t bits = bm[w];
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    rowidxC[pos] = i;
-                    colidxC[pos] = (wlo + w) * 32 + b;
-                    pos++;
-                    bits &= bits - 1u;
-                }
-            }
+        for (int k = lane; k < n; k += 32) {
+            colidxC[t0 + k] = slot_col[s0 + k];
+            rowidxC[t0 + k] = i;
         }
-        __syncthreads();
     }
 }
 
@@ -718,7 +695,7 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     if (tilem > 0 && numtileC > 0) {
         c1_fill_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                               B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
-                                                              C->tile_colidxC);
+                                                              C->tile_colidxC, nullptr);
         SPG_CUDA(h, cudaGetLastError());
     }
     spg_free_async(h, cnt);
@@ -726,57 +703,69 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     return SPG_OK;
 }
 
-// Step 1 with C's tile arrays pre-sized to `cap` tiles (learned sizing): one
-// fused bitmap pass; if the capacity was too small the exact fill re-runs.
+// Step 1 with learned sizing: slot_sz[i] is the predicted tile count of
+// tile-row i (with margin).  Slots are laid out by a scan, filled in one
+// bitmap pass, then compacted into C's exact arrays; rows whose prediction
+// was too small re-run the exact fill.  The structure is exact whatever the
+// prediction.
 spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                             int64_t* row_pairs, unsigned long long* pairs_total, int64_t cap) {
+                             int64_t* row_pairs, unsigned long long* pairs_total, const int* slot_sz) {
     const int tilem = A->tilem;
     const int nwords = (B->tilen + 31) / 32;
     const size_t smem = sizeof(uint32_t) * (size_t)nwords;
     if (smem > h->smem_optin)
         return spg_fail(h, SPG_ERR_UNSUPPORTED, "step 1: B has too many tile columns for one bitmap");
-    SPG_CUDA(h, cudaFuncSetAttribute(c1_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SPG_CUDA(h, cudaFuncSetAttribute(c1_slot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SPG_CUDA(h, cudaFuncSetAttribute(c1_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (cap < 1) cap = 1;
-    SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
-    SPG_TRY(spg_alloc_t(h, &C->tile_rowidxC, (size_t)cap + 1));
-    SPG_TRY(spg_alloc_t(h, &C->tile_colidxC, (size_t)cap + 1));
-    unsigned long long* state = nullptr;
-    SPG_TRY(spg_alloc_t(h, &state, (size_t)tilem + 2));
-    SPG_CUDA(h, cudaMemsetAsync(state, 0, sizeof(unsigned long long) * ((size_t)tilem + 2), h->stream));
-    SPG_CUDA(h, cudaMemsetAsync(C->tile_ptrC, 0, sizeof(int) * ((size_t)tilem + 1), h->stream));
+    int64_t* slot_off = nullptr;
+    SPG_TRY(spg_alloc_t(h, &slot_off, (size_t)tilem + 1));
+    SPG_TRY(spg_scan_i32_to_i64(h, slot_sz, slot_off, tilem));
+    int64_t cap = 0;
+    SPG_TRY(spg_read_i64(h, slot_off + tilem, &cap));
+    h->stats.predicted_tiles = cap;
+    int* slot_col = nullptr;
+    int* cnt = nullptr;
+    int64_t* ptr64 = nullptr;
+    SPG_TRY(spg_alloc_t(h, &slot_col, (size_t)cap + 1));
+    SPG_TRY(spg_alloc_t(h, &cnt, (size_t)tilem + 1));
+    SPG_TRY(spg_alloc_t(h, &ptr64, (size_t)tilem + 1));
     if (tilem > 0) {
-        int occ = 1;
-        SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c1_fused_kernel, C1_THREADS, smem));
-        int grid = h->num_sms * (occ < 1 ? 1 : occ);
-        if (grid > tilem) grid = tilem;
-        c1_fused_kernel<<<grid, C1_THREADS, smem, h->stream>>>(
-            tilem, A->tile_ptr, A->tile_columnidx, B->tile_ptr, B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
-            C->tile_colidxC, cap, row_pairs, pairs_total, state, reinterpret_cast<unsigned*>(state + tilem + 1),
-            h->d_flags);
+        c1_slot_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(A->tile_ptr, A->tile_columnidx, B->tile_ptr,
+                                                              B->tile_columnidx, slot_off, slot_col, cnt, row_pairs,
+                                                              pairs_total);
         SPG_CUDA(h, cudaGetLastError());
     }
-    int numtileC = 0;
-    SPG_TRY(spg_read_i32(h, C->tile_ptrC + tilem, &numtileC));
-    spg_free_async(h, state);
-    unsigned fl = 0;
-    SPG_CUDA(h, cudaMemcpy(&fl, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
-    if (fl & (DERR_TIMEOUT | DERR_TOO_BIG)) return spg_check_flags(h, "step 1");
+    SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
+    int64_t numtileC = 0;
+    SPG_TRY(spg_read_i64(h, ptr64 + tilem, &numtileC));
+    if (numtileC > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "C has more than 2^31-1 tiles");
     C->numtileC = numtileC;
-    if (fl & DERR_OVERFLOW) {  // prediction too small: exact re-run of the fill
-        SPG_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
-        h->stats.overflow_reruns++;
-        spg_free_async(h, C->tile_rowidxC);
-        spg_free_async(h, C->tile_colidxC);
-        SPG_TRY(spg_alloc_t(h, &C->tile_rowidxC, (size_t)numtileC + 1));
-        SPG_TRY(spg_alloc_t(h, &C->tile_colidxC, (size_t)numtileC + 1));
-        if (tilem > 0 && numtileC > 0) {
-            c1_fill_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
-                                                                  B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
-                                                                  C->tile_colidxC);
+    SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
+    i64_to_i32_kernel<<<grid_cap(h, tilem + 1, 256, 8), 256, 0, h->stream>>>(ptr64, C->tile_ptrC, tilem + 1);
+    SPG_CUDA(h, cudaGetLastError());
+    SPG_TRY(spg_alloc_t(h, &C->tile_rowidxC, (size_t)numtileC + 1));
+    SPG_TRY(spg_alloc_t(h, &C->tile_colidxC, (size_t)numtileC + 1));
+    int* over_rows = cnt;  // reused: counts are no longer needed
+    unsigned* n_over = reinterpret_cast<unsigned*>(ptr64);
+    SPG_CUDA(h, cudaMemsetAsync(n_over, 0, sizeof(unsigned), h->stream));
+    if (tilem > 0 && numtileC > 0) {
+        c1_compact_kernel<<<grid_cap(h, (int64_t)tilem * 32, 256, 16), 256, 0, h->stream>>>(
+            tilem, C->tile_ptrC, slot_off, slot_col, C->tile_rowidxC, C->tile_colidxC, over_rows, n_over);
+        SPG_CUDA(h, cudaGetLastError());
+        int nov = 0;
+        SPG_TRY(spg_read_i32(h, reinterpret_cast<const int*>(n_over), &nov));
+        if (nov > 0) {  // prediction too small for these rows: exact fill of just them
+            h->stats.overflow_reruns += nov;
+            c1_fill_kernel<<<nov, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
+                                                                B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
+                                                                C->tile_colidxC, over_rows);
             SPG_CUDA(h, cudaGetLastError());
         }
     }
+    spg_free_async(h, slot_off);
+    spg_free_async(h, slot_col);
+    spg_free_async(h, cnt);
+    spg_free_async(h, ptr64);
     return SPG_OK;
 }
 

@@ -16,9 +16,9 @@ struct PlainPriv {
 spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                        int64_t* row_pairs, unsigned long long* pairs_total);
 spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                             int64_t* row_pairs, unsigned long long* pairs_total, int64_t cap);
-spg_status mlp_predict_capacity(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int64_t* cap_tiles,
-                                int64_t* cap_nnz);
+                             int64_t* row_pairs, unsigned long long* pairs_total, const int* slot_sz);
+// Per tile-row slot sizes (predicted C tiles with margin) from the sizing MLP.
+spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz);
 spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                        PlainPriv* pp, int* tile_cnt);
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,

@@ -257,10 +257,12 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
     SPG_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
     // ---- step 1: C tile structure
     if (h->sizing) {
-        int64_t cap_t = 0, cap_z = 0;
-        SPG_TRY(mlp_predict_capacity(h, A, B, &cap_t, &cap_z));
-        h->stats.predicted_tiles = cap_t;
-        SPG_TRY(plain_step1_sized(h, A, B, C, cp->row_pairs, cp->plain.counters + 2, cap_t));
+        int* slot = nullptr;
+        SPG_TRY(spg_alloc_t(h, &slot, (size_t)A->tilem + 1));
+        SPG_TRY(mlp_predict_rows(h, A, B, slot));
+        const spg_status st = plain_step1_sized(h, A, B, C, cp->row_pairs, cp->plain.counters + 2, slot);
+        spg_free_async(h, slot);
+        SPG_TRY(st);
     } else {
         SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
     }

@@ -129,7 +129,7 @@ typedef struct {
     float ms_step2;             /* bitmask symbolic + scan + ptrRowC           */
     float ms_step3;             /* numeric                                     */
     int64_t products;           /* sum over A nonzeros of nnz(B row)           */
-    int64_t overflow_reruns;    /* pre-sized buffers that had to be re-run     */
+    int64_t overflow_reruns;    /* re-runs: pair cache, or tile-rows that outgrew their predicted slot */
     int64_t work_items;         /* row-wise windows launched                   */
     int64_t tensor_pairs;       /* tile pairs computed on tensor cores         */
     int64_t fp64_tiles;         /* C tiles recomputed in FP64                  */
@@ -305,9 +305,11 @@ spg_status spg_batch_set_bins(spg_handle_t h, spg_batch_t b, int n_thresholds, c
  * a host read-back before filling (src/spgemm_raw_v2.cu:119-156).  An MLP
  * (8 per-tile-row features -> 32 -> 32 -> 2) predicts each C tile-row's tile
  * count and nonzeros; with a model attached (spg_set_sizing_model) step 1
- * pre-sizes C from the predicted total and runs as one fused pass, the exact
- * count inside it judging the prediction (too small => exact re-run of the
- * fill; stats.overflow_reruns).  The model is trained on the GPU by
+ * gives every C tile-row a slot of its predicted size, builds each row's
+ * bitmap once (exact count, tiles written into the slot) and compacts the
+ * slots into C's exact arrays; a row whose slot was too small re-runs the
+ * exact fill (stats.overflow_reruns counts those rows).  The structure is
+ * exact whatever the prediction.  The model is trained on the GPU by
  * spg_mlp_train (forward, backward and Adam kernels of this library). */
 typedef struct spg_mlp_s* spg_mlp_t;
 int spg_mlp_num_params(void);

@@ -1,5 +1,5 @@
 """Learned sizing: CUDA MLP gradients against the numpy restatement; training
-lowers the loss; with the trained model attached step 1 runs as one fused
+lowers the loss; with the trained model attached step 1 runs as one slotted
 pass with the exact same C structure; a model that under-predicts triggers
 the exact re-run and still gives the exact structure."""
 import os
@@ -69,8 +69,11 @@ def test_trained_sizing_single_pass_same_structure(handle, name, a):
     for k in KEYS:
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
     assert st0["predicted_tiles"] == 0
-    assert st1["predicted_tiles"] >= got["numtileC"]   # the trained model sized C: one fused pass
-    assert st1["overflow_reruns"] == 0
+    assert st1["predicted_tiles"] >= got["numtileC"]   # the trained model's slots hold all of C
+    # one bitmap pass fills the predicted slots; only a few tile-rows outgrow
+    # theirs and re-run the exact fill
+    busy = int(np.count_nonzero(np.diff(got["tile_ptrC"])))
+    assert st1["overflow_reruns"] <= max(1, busy // 20), (st1["overflow_reruns"], busy)
     model.free()
 
 
