@@ -519,7 +519,8 @@ def main():
     p.add_argument("--batch-count", type=int, default=512)
     p.add_argument("--check", action="store_true", help="value error vs the FP64 oracle on a prefix of C")
     p.add_argument("--sizing", type=int, default=1, help="attach the trained sizing MLP (1) or not (0)")
-    p.add_argument("--sizing-margin", type=float, default=0.25)
+    p.add_argument("--sizing-margin", type=float, default=1.0,
+                   help="slot of a tile-row = predicted tiles * (1 + margin) + 2")
     p.add_argument("--traffic", type=float, default=None,
                    help="dram bytes per launch of the dominant kernel from an ncu capture")
     args = p.parse_args()

@@ -492,7 +492,7 @@ class SizingModel:
                                                         C.byref(loss)))
         return loss.value
 
-    def attach(self, margin: float = 0.25):
+    def attach(self, margin: float = 1.0):
         self.handle.check(self.handle.lib.spg_set_sizing_model(self.handle.h, self.m, margin))
 
     def detach(self):

@@ -73,7 +73,7 @@ __device__ __forceinline__ T block_excl_scan(T v, T* sh, T* total) {
 struct spg_handle_s {
     int device = 0;
     struct spg_mlp_s* sizing = nullptr;  // learned sizing model (optional)
-    float sizing_margin = 0.25f;
+    float sizing_margin = 1.0f;
     int dense_thr = 32;        // tile nnz above which a tile pair goes to tensor cores (MIXED)
     float cancel_eps = 9.5367431640625e-07f;  // 2^-20: |c| < eps * sum|a||b| flags a C tile for FP64
     cudaStream_t stream = nullptr;

@@ -331,7 +331,8 @@ spg_status spg_mlp_gradient(spg_handle_t h, spg_mlp_t m, const float* d_feat, co
    indices (NULL = in order). */
 spg_status spg_mlp_train(spg_handle_t h, spg_mlp_t m, const float* d_feat, const float* d_target, int64_t n,
                          const int* d_perm, int epochs, int batch, float lr, float* last_epoch_loss);
-/* Attach (m) or detach (NULL) the sizing model; capacity = prediction * (1+margin). */
+/* Attach (m) or detach (NULL) the sizing model; slot of a tile-row = prediction * (1+margin) + 2
+   tiles (1.0 is a good margin: slots cost 4 bytes a tile, re-filled rows a bitmap pass). */
 spg_status spg_set_sizing_model(spg_handle_t h, spg_mlp_t m, float margin);
 
 /* Intermediate products sum_{(i,k) in A} nnz(B(k,:)) (src/spgemm_raw_v2.cu:95-99),
