@@ -356,10 +356,15 @@ def measure_e2e(h, api, a, b, args, flops, stream):
     """End to end through the C ABI with host buffers, per step: the CSR inputs
     are copied from pinned host memory to the device and tiled, C = A*B is
     computed, and every array of C is copied back to pinned host memory.  C can
-    exceed host memory (R-MAT 2^20: ~160 GB), so it streams through a fixed
-    pinned staging area in tile ranges (spg_ctiles_to_host_range)."""
-    import torch
+    exceed host memory (R-MAT 2^20: ~160 GB), so it streams through fixed
+    pinned staging areas in tile ranges (spg_ctiles_to_host_range).  C's
+    structure is final when spg_symbolic returns, so copy workers (each with
+    its own handle, stream and staging) take tile ranges of it from a shared
+    counter while spg_numeric runs; the values follow when the numeric phase
+    ends, on the same workers."""
+    import threading
     import ctypes as C
+    import torch
     from gpu_spgemm_gb300 import _lib as L
 
     def pin(x):
@@ -371,12 +376,69 @@ def measure_e2e(h, api, a, b, args, flops, stream):
     code = L.SPG_F64 if a.val.dtype == np.float64 else L.SPG_F32
     vd = np.float64 if code == L.SPG_F64 else np.float32
     h2d = sum(x[1].nbytes for x in ha + hb)
-    CT = 1 << 24            # C tiles per staged range
-    VC = 1 << 28            # values per staged range
-    st = dict(r=pin(np.zeros(CT, np.int32)), c=pin(np.zeros(CT, np.int32)), m=pin(np.zeros(CT * TS, np.uint16)),
-              p=pin(np.zeros(CT + 1, np.int64)), pr=pin(np.zeros(CT * TS, np.uint8)),
-              v=pin(np.zeros(VC, vd)), cc=pin(np.zeros(VC, np.uint8)), tp=None)
+    CT = 1 << 23            # C tiles per staged range
+    VC = 1 << 27            # values per staged range (ranges halve when a range holds more)
+    NW = max(1, args.e2e_copy_workers)
     lib = h.lib
+
+    class Worker:
+        def __init__(self):
+            self.stream = torch.cuda.Stream()
+            self.h = api.Handle(torch.cuda.current_device(), self.stream)
+            self.st = dict(r=pin(np.zeros(CT, np.int32)), c=pin(np.zeros(CT, np.int32)),
+                           m=pin(np.zeros(CT * TS, np.uint16)), p=pin(np.zeros(CT + 1, np.int64)),
+                           pr=pin(np.zeros(CT * TS, np.uint8)), v=pin(np.zeros(VC, vd)),
+                           cc=pin(np.zeros(VC, np.uint8)))
+
+    workers = [Worker() for _ in range(NW)]
+    tstat = {}
+
+    def run_workers(c, want_struct):
+        """Copies C's structure (want_struct) or values in tile ranges taken
+        from a shared counter by every worker; returns the bytes copied."""
+        lock = threading.Lock()
+        nxt = [0]
+        nb = [0]
+        errs = []
+
+        def work(wk):
+            nv = C.c_int64()
+            g = lambda k: wk.st[k][1].ctypes.data
+            try:
+                while True:
+                    with lock:
+                        t0 = nxt[0]
+                        if t0 >= c.numtileC:
+                            return
+                        t1 = min(c.numtileC, t0 + CT)
+                        nxt[0] = t1
+                    while t0 < t1:  # a value range holding more than VC values is cut in halves
+                        step = t1 - t0
+                        while True:
+                            e = min(t1, t0 + step)
+                            if want_struct:
+                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, g("r"), g("c"), g("m"),
+                                                                  g("p"), g("pr"), None, None, VC, C.byref(nv))
+                            else:
+                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, None, None,
+                                                                  None, g("v"), g("cc"), VC, C.byref(nv))
+                            if s_ == L.SPG_ERR_INVALID and not want_struct and step > 1:
+                                step //= 2
+                                continue
+                            wk.h.check(s_)
+                            break
+                        b_ = (e - t0) * (4 + 4 + 32 + 8 + 16) + 8 if want_struct else \
+                            nv.value * (np.dtype(vd).itemsize + 1)
+                        with lock:
+                            nb[0] += b_
+                        t0 = e
+            except Exception as ex:
+                errs.append(ex)
+
+        ths = [threading.Thread(target=work, args=(wk,)) for wk in workers]
+        for t in ths:
+            t.start()
+        return ths, nb, errs
 
     def one():
         ta, tb, c = L.SpgTiles(), L.SpgTiles(), L.SpgCTiles()
@@ -384,32 +446,29 @@ def measure_e2e(h, api, a, b, args, flops, stream):
                                            ha[2][1].ctypes.data, code, L.SPG_LAYOUT_ROW, 0, C.byref(ta)))
         h.check(lib.spg_tile_from_csr_host(h.h, b.m, b.n, b.nnz, hb[0][1].ctypes.data, hb[1][1].ctypes.data,
                                            hb[2][1].ctypes.data, code, L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
-        h.check(lib.spg_spgemm(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], api._PRECS[args.prec],
-                               C.byref(c)))
+        h.check(lib.spg_symbolic(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], C.byref(c)))
         tp = np.zeros(c.tilem + 1, np.int32)
         h.check(lib.spg_ctiles_to_host(h.h, C.byref(c), tp.ctypes.data, None, None, None, None, None, None, None))
-        d2h = tp.nbytes
-        nt = c.numtileC
-        t0 = 0
-        step = CT
-        nv = C.c_int64()
-        while t0 < nt:
-            t1 = min(nt, t0 + step)
-            s_ = lib.spg_ctiles_to_host_range(h.h, C.byref(c), t0, t1, st["r"][1].ctypes.data,
-                                              st["c"][1].ctypes.data, st["m"][1].ctypes.data,
-                                              st["p"][1].ctypes.data, st["pr"][1].ctypes.data,
-                                              st["v"][1].ctypes.data, st["cc"][1].ctypes.data, VC, C.byref(nv))
-            if s_ == L.SPG_ERR_INVALID and step > 1:
-                step //= 2
-                continue
-            h.check(s_)
-            d2h += (t1 - t0) * (4 + 4 + 32 + 8 + 16) + 8 + nv.value * (np.dtype(vd).itemsize + 1)
-            t0 = t1
-            step = CT
+        t = time.perf_counter()
+        ths, nbs, errs = run_workers(c, True)
+        h.check(lib.spg_numeric(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], api._PRECS[args.prec],
+                                C.byref(c)))
+        t_num = time.perf_counter()
+        for th in ths:
+            th.join()
+        t_struct = time.perf_counter()
+        ths2, nbv, errs2 = run_workers(c, False)
+        for th in ths2:
+            th.join()
+        t_val = time.perf_counter()
+        if errs or errs2:
+            raise (errs + errs2)[0]
+        tstat.update(numeric_ms=(t_num - t) * 1e3, structure_copy_ms=(t_struct - t) * 1e3,
+                     values_copy_ms=(t_val - t_struct) * 1e3)
         lib.spg_ctiles_free(h.h, C.byref(c))
         lib.spg_tiles_free(h.h, C.byref(ta))
         lib.spg_tiles_free(h.h, C.byref(tb))
-        return d2h
+        return tp.nbytes + nbs[0] + nbv[0]
 
     try:
         one()
@@ -422,12 +481,16 @@ def measure_e2e(h, api, a, b, args, flops, stream):
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / steps
         return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": dt * 1e3, "steps": steps,
-                "path": "spg_tile_from_csr_host x2 + spg_spgemm + spg_ctiles_to_host(_range) into pinned host "
-                        "staging (%d tiles / %d values per range)" % (CT, VC)}
+                "ms_per_step": dt * 1e3, "steps": steps, "last_step": {k: round(v, 1) for k, v in tstat.items()},
+                "path": "spg_tile_from_csr_host x2 + spg_symbolic + spg_numeric; C to pinned host staging by "
+                        "spg_ctiles_to_host_range on %d copy handles/streams: structure during the numeric "
+                        "phase, values after it (%d tiles per range)" % (NW, CT)}
     except Exception as e:  # report instead of dying
         return {"value": None, "unit": "GFLOP/s", "error": str(e)[:200], "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": None}
+    finally:
+        for wk in workers:
+            wk.h.close()
 
 
 def run_batch(args):
@@ -514,6 +577,8 @@ def main():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--e2e-copy-workers", type=int, default=2,
+                   help="copy handles/streams/host threads streaming C back in the e2e measurement")
     p.add_argument("--cpu-s", type=float, default=12.0)
     p.add_argument("--ref-step-s", type=float, default=8.0)
     p.add_argument("--batch-count", type=int, default=512)
