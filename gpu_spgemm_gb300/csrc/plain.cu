@@ -172,7 +172,7 @@ c1_slot_kernel(const int* __restrict__ a_tp, const int* __restrict__ a_tc, const
         uint32_t bits = bm[w];
         while (bits) {
             const int b = __ffs(bits) - 1;
-            slot_col[pos++] = (wlo + w) * 32 + b;
+            __stcs(&slot_col[pos++], (wlo + w) * 32 + b);
             bits &= bits - 1u;
         }
     }
@@ -194,8 +194,8 @@ __global__ void c1_compact_kernel(int tilem, const int* __restrict__ tile_ptrC, 
             continue;
         }
         for (int k = lane; k < n; k += 32) {
-            colidxC[t0 + k] = slot_col[s0 + k];
-            rowidxC[t0 + k] = i;
+            __stcs(&colidxC[t0 + k], __ldcs(&slot_col[s0 + k]));
+            __stcs(&rowidxC[t0 + k], i);
         }
     }
 }

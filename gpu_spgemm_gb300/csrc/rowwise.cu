@@ -20,7 +20,9 @@
 //   window to window, so B's rows are read once per region, never searched
 //   per window;
 //   a B entry (c, v) finds its C tile by a popcount rank in a bitmap of the
-//   window's tile columns, its value slot by popc of the C row mask.
+//   window's tile columns, its value slot by popc of the C row mask;
+//   C's arrays stream through L2 once (evict-first loads and stores), so the
+//   re-read B rows keep the cache.
 #include <climits>
 
 #include "rowwise.cuh"
@@ -182,7 +184,7 @@ __device__ void build_window_rank(const int* __restrict__ colidxC, int t0, int n
     for (int x = threadIdx.x; x < nwd; x += RW_THREADS) bp[x] = make_uint2(0u, 0u);
     __syncthreads();
     for (int x = threadIdx.x; x < nt; x += RW_THREADS) {
-        const int j = colidxC[t0 + x];
+        const int j = __ldcs(&colidxC[t0 + x]);
         atomicOr(&bp[(j >> 5) - wlo].x, 1u << (j & 31));
     }
     __syncthreads();
@@ -429,10 +431,10 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                 }
                 const int64_t t = (int64_t)w0 + x;
                 uint4* mo = reinterpret_cast<uint4*>(maskC) + 2 * t;
-                mo[0] = make_uint4(mw[0], mw[1], mw[2], mw[3]);
-                mo[1] = make_uint4(mw[4], mw[5], mw[6], mw[7]);
-                reinterpret_cast<uint4*>(ptrRowC)[t] = make_uint4(pw[0], pw[1], pw[2], pw[3]);
-                tile_cnt[t] = tot;
+                __stcs(mo, make_uint4(mw[0], mw[1], mw[2], mw[3]));
+                __stcs(mo + 1, make_uint4(mw[4], mw[5], mw[6], mw[7]));
+                __stcs(reinterpret_cast<uint4*>(ptrRowC) + t, make_uint4(pw[0], pw[1], pw[2], pw[3]));
+                __stcs(&tile_cnt[t], tot);
             }
             __syncthreads();
         }
@@ -495,8 +497,8 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             const int limit = (jhi + 1) * TS;
             for (int x = tid; x < ntw * TS; x += RW_THREADS) {
                 const int64_t t = (int64_t)t0 + (x >> 4);
-                const uint32_t base = (uint32_t)(tile_nnzC[t] - v0) + ptrRowC[(int64_t)t0 * TS + x];
-                words[x] = (base << 16) | maskC[(int64_t)t0 * TS + x];
+                const uint32_t base = (uint32_t)(tile_nnzC[t] - v0) + __ldcs(&ptrRowC[(int64_t)t0 * TS + x]);
+                words[x] = (base << 16) | __ldcs(&maskC[(int64_t)t0 * TS + x]);
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             if (tid == 0) s_fx = 0;
@@ -513,11 +515,11 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                 const uint8_t rb = (uint8_t)((x & 15) << 4);
                 while (m16) {
                     const int c = __clz(m16) - 16;
-                    *o++ = rb | (uint8_t)c;
+                    __stcs(o++, (uint8_t)(rb | (uint8_t)c));
                     m16 &= ~(0x8000u >> c);
                 }
             }
-            for (int x = tid; x < nv; x += RW_THREADS) valC[v0 + x] = (V)acc[x];
+            for (int x = tid; x < nv; x += RW_THREADS) __stcs(&valC[v0 + x], (V)acc[x]);
             __syncthreads();
             t0 = t1;
         }
