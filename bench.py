@@ -39,6 +39,11 @@ from gpu_spgemm_gb300 import synth  # noqa: E402
 L2_BYTES = 129 * 1024 * 1024
 TS = 16
 
+# DRAM bytes per launch of the dominant kernel, from one-pass ncu captures of
+# the same bench command (dram__bytes_read.sum + dram__bytes_write.sum), by
+# (workload, step); profiles/traffic_rmat20.md holds the capture.
+MEASURED_TRAFFIC = {("rmat20", "step3"): 276.96e9 + 79.38e9}
+
 
 def workload(name: str):
     if name == "rmat20":
@@ -264,13 +269,13 @@ def run_ours(args):
                  "step2": sym_bytes, "step3": num_bytes}[dom]
     achieved = dom_bytes / (steps_ms[dom] * 1e-3) / 1e9
     rowwise = stats[-1].get("algo_used", 1) == 2
-    names = {"step1": "c1_count_kernel + c1_fill_kernel",
+    names = {"step1": "c1_slot_kernel + c1_compact_kernel" if args.sizing else "c1_count_kernel + c1_fill_kernel",
              "step2": "rw_symbolic_kernel" if rowwise else "c2_symbolic_kernel",
              "step3": "rw_numeric_kernel" if rowwise else "c3_numeric_kernel"}
     roofline = {"bound": "hbm", "kernel": names[dom],
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "peak_source": peak_src, "algorithmic_bytes": dom_bytes, "ms": steps_ms[dom],
-                "traffic": args.traffic}
+                "traffic": args.traffic if args.traffic is not None else MEASURED_TRAFFIC.get((args.workload, dom))}
     total_bytes = a_b + b_b + c_b
     hbm_steps = total_bytes / (ms * 1e-3) / 1e9
 
