@@ -15,7 +15,9 @@
 //   persistent CTAs take items from an atomic ticket (biggest tile-rows first,
 //   in natural order);
 //   a region is walked in shared-memory windows (symbolic: WS tiles of 16 row
-//   masks; numeric: <= NW_MAXT tiles and <= NW_VALS values of C);
+//   masks; numeric: as many C tiles as fit one shared-memory arena at 64 bytes
+//   of metadata a tile plus one accumulator a value, so windows of dense C
+//   tiles hold more values and windows of sparse ones more tiles);
 //   per A nonzero of the tile-row a cursor into its B row carries over from
 //   window to window, so B's rows are read once per region, never searched
 //   per window;
@@ -33,8 +35,11 @@ constexpr int RW_THREADS = 512;
 constexpr int RW_WARPS = RW_THREADS / 32;
 constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
-constexpr int NW_MAXT = 768;    // C tiles per numeric window
-constexpr int NW_VALS = 6144;   // C values per numeric window
+// numeric window arena (bytes): 64 B of row words a tile + sizeof(ACC) a value
+constexpr int NW_ARENA_F32 = 74752;   // two blocks per SM
+constexpr int NW_ARENA_F64 = 131072;  // one block per SM
+template <typename ACC>
+constexpr int nw_arena() { return sizeof(ACC) == 4 ? NW_ARENA_F32 : NW_ARENA_F64; }
 constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose cursors fit in shared memory
 constexpr int SWU = 4;          // 32-product steps per sweep round of a warp (loads in flight)
 
@@ -457,9 +462,9 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
                   unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
-    ACC* acc = reinterpret_cast<ACC*>(smem);                                   // NW_VALS + 256
-    uint32_t* words = reinterpret_cast<uint32_t*>(acc + NW_VALS + 256);        // [NW_MAXT][16]
-    int* cur_s = reinterpret_cast<int*>(words + NW_MAXT * TS);                 // 4 x MAXA_SMEM
+    constexpr int ARENA = nw_arena<ACC>();
+    uint32_t* words = smem;                                                    // [ntw][16], then acc[nv]
+    int* cur_s = reinterpret_cast<int*>(reinterpret_cast<char*>(smem) + ARENA); // 4 x MAXA_SMEM
     uint2* bp = reinterpret_cast<uint2*>(cur_s + 4 * MAXA_SMEM);               // nwords_b
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
@@ -474,13 +479,15 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
         init_cursors(it, cu, colidxC, a_ci, b_rp, b_ci);
         int t0 = it.rs;
         while (t0 < it.re) {
-            // window [t0, t1): at most NW_MAXT tiles and NW_VALS values (a tile holds <= 256)
+            // window [t0, t1): the longest run of tiles whose row words and
+            // values fit the arena (one tile always fits: 64 + 256 values)
             const int64_t v0 = tile_nnzC[t0];
-            const int cap_t = min(NW_MAXT, it.re - t0);
+            const int cap_t = min(ARENA / 64, it.re - t0);
             if (tid == 0) s_nt = 0;
             __syncthreads();
             int ok = 0;
-            for (int x = tid; x < cap_t; x += RW_THREADS) ok += (tile_nnzC[t0 + x + 1] - v0 <= NW_VALS) ? 1 : 0;
+            for (int x = tid; x < cap_t; x += RW_THREADS)
+                ok += (64 * (int64_t)(x + 1) + (int64_t)sizeof(ACC) * (tile_nnzC[t0 + x + 1] - v0) <= ARENA) ? 1 : 0;
             if (ok) atomicAdd(&s_nt, ok);
             __syncthreads();
             const int ntw = max(1, s_nt);
@@ -495,6 +502,7 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             const int jlo = colidxC[t0], jhi = colidxC[t1 - 1];
             const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
             const int limit = (jhi + 1) * TS;
+            ACC* acc = reinterpret_cast<ACC*>(words + ntw * TS);
             for (int x = tid; x < ntw * TS; x += RW_THREADS) {
                 const int64_t t = (int64_t)t0 + (x >> 4);
                 const uint32_t base = (uint32_t)(tile_nnzC[t] - v0) + __ldcs(&ptrRowC[(int64_t)t0 * TS + x]);
@@ -532,8 +540,7 @@ size_t sym_smem(int nwords_b) {
 
 template <typename ACC>
 size_t num_smem(int nwords_b) {
-    return (size_t)(NW_VALS + 256) * sizeof(ACC) + (size_t)NW_MAXT * TS * 4 + (size_t)MAXA_SMEM * 16 +
-           (size_t)nwords_b * 8;
+    return (size_t)nw_arena<ACC>() + (size_t)MAXA_SMEM * 16 + (size_t)nwords_b * 8;
 }
 
 }  // namespace
