@@ -417,7 +417,12 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             const int jlo = colidxC[w0], jhi = colidxC[w0 + nt - 1];
             const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
             const int limit = (jhi + 1) * TS;
-            for (int x = tid; x < WS * 8; x += RW_THREADS) masks32[x] = 0u;
+            {  // clear the window's 16 rows of masks (nt halfwords each), one warp a row
+                static_assert(RW_WARPS == TS, "one warp per tile row");
+                const int nh = (nt + 1) >> 1;
+                uint32_t* row = masks32 + (tid >> 5) * (WS / 2);
+                for (int w = tid & 31; w < nh; w += 32) row[w] = 0u;
+            }
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bp, s_sh);
             walk_window(it, cu, s_rows, limit, b_ci, &s_fx, SymOp{bp, wlo, masks32});
