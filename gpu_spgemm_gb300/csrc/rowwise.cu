@@ -508,10 +508,28 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
             const int limit = (jhi + 1) * TS;
             ACC* acc = reinterpret_cast<ACC*>(words + ntw * TS);
-            for (int x = tid; x < ntw * TS; x += RW_THREADS) {
-                const int64_t t = (int64_t)t0 + (x >> 4);
-                const uint32_t base = (uint32_t)(tile_nnzC[t] - v0) + __ldcs(&ptrRowC[(int64_t)t0 * TS + x]);
-                words[x] = (base << 16) | __ldcs(&maskC[(int64_t)t0 * TS + x]);
+            // row words, one thread per tile: 2 x 16 B of masks, 16 B of row
+            // offsets and the tile's value offset, all loads in flight at once
+            for (int lt = tid; lt < ntw; lt += RW_THREADS) {
+                const int64_t t = (int64_t)t0 + lt;
+                const uint4 m0 = __ldcs(reinterpret_cast<const uint4*>(maskC) + 2 * t);
+                const uint4 m1 = __ldcs(reinterpret_cast<const uint4*>(maskC) + 2 * t + 1);
+                const uint4 po = __ldcs(reinterpret_cast<const uint4*>(ptrRowC) + t);
+                const uint32_t vb = (uint32_t)(tile_nnzC[t] - v0);
+                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+                const uint32_t pw[4] = {po.x, po.y, po.z, po.w};
+                uint32_t w[16];
+#pragma unroll
+                for (int r = 0; r < TS; r++) {
+                    const uint32_t m16 = (mw[r >> 1] >> (16 * (r & 1))) & 0xffffu;
+                    const uint32_t off = vb + ((pw[r >> 2] >> (8 * (r & 3))) & 0xffu);
+                    w[r] = (off << 16) | m16;
+                }
+                uint4* dst = reinterpret_cast<uint4*>(words + lt * TS);
+                dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                dst[2] = make_uint4(w[8], w[9], w[10], w[11]);
+                dst[3] = make_uint4(w[12], w[13], w[14], w[15]);
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             if (tid == 0) s_fx = 0;
