@@ -130,6 +130,24 @@ def dist_setup():
     return world, rank, local
 
 
+def job_time_and_value(ms_local: float, flops_local: float, world: int, device) -> tuple:
+    """Whole-job figures of a replicas-only run: every rank multiplies its own
+    copy of the workload between two barriers, so the job's step time is the
+    slowest rank's and its work is the sum of the ranks' work.  Returns
+    (ms per step, GFLOP/s of the whole job).  Works on any process-group
+    backend (NCCL on the GPUs, gloo on CPU)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    f = torch.tensor([flops_local], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(f, op=dist.ReduceOp.SUM)
+        dist.barrier()
+    ms = float(t.item())
+    return ms, float(f.item()) / (ms * 1e-3) / 1e9
+
+
 def cpu_gflops(a, b, target_s: float = 12.0, dtype=np.float32):
     """OpenMP Gustavson on a seeded stride sample of A's rows, sized to about
     target_s seconds; returns (GFLOP/s, threads, sample description)."""
@@ -236,14 +254,8 @@ def run_ours(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    ms = float(t.item())
+    ms, value = job_time_and_value(ev0.elapsed_time(ev1) / args.steps, flops, world, "cuda")
     numtileC, nnzC, pairs = info
-    value = world * flops / (ms * 1e-3) / 1e9
 
     # ---- roofline of the dominant kernel (CUDA events around it inside the library)
     peaks = {}
@@ -507,6 +519,9 @@ def run_batch(args):
     from gpu_spgemm_gb300 import api
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     count = args.batch_count
     pairs = synth.er_batch(count)
     stream = torch.cuda.Stream()
@@ -550,7 +565,7 @@ def run_batch(args):
     ms_graph = timed(bt.graph_launch, args.steps)
     h2d = sum(x.nbytes for x in new_a + new_b)
     d2h = sum(int(z) * 4 for z in nz)
-    value = flops / (ms_batch * 1e-3) / 1e9
+    ms_batch, value = job_time_and_value(ms_batch, flops, world, "cuda")
     line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "float32", "data": "synthetic",
