@@ -35,7 +35,8 @@ constexpr int RW_THREADS = 512;
 constexpr int RW_WARPS = RW_THREADS / 32;
 constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
-// numeric window arena (bytes): 64 B of row words a tile + sizeof(ACC) a value
+// numeric window arena (bytes): 8 B a tile + 4 B a non-empty tile row +
+// sizeof(ACC) a value
 constexpr int NW_ARENA_F32 = 74752;   // two blocks per SM
 constexpr int NW_ARENA_F64 = 131072;  // one block per SM
 template <typename ACC>
@@ -362,15 +363,18 @@ struct SymOp {
     }
 };
 
-// Numeric product: a_ik * b_kc into C's value slot.  A window's C tile rows
-// are one word each, (value offset of the row << 16) | row mask.
+// Numeric product: a_ik * b_kc into C's value slot.  A window's C tiles are
+// one uint2 each, {value offset of the tile, (first row word << 16) | mask of
+// its non-empty rows}; each non-empty row is one word, (value offset of the
+// row << 16) | row mask.
 template <typename V, typename ACC>
 struct NumOp {
     struct Entry { ACC va; };
     struct Loaded { ACC vb; };
     const uint2* bp;
     int wlo;
-    const uint32_t* words;
+    const uint2* tinfo;
+    const uint32_t* rows;
     ACC* acc;
     const V* a_val;
     const V* b_val;
@@ -383,7 +387,8 @@ struct NumOp {
         return Loaded{p >= 0 ? (ACC)__ldg(&b_val[p]) : ACC(0)};
     }
     __device__ __forceinline__ void apply(int r, int c, Entry e, Loaded l) const {
-        const uint32_t w = words[wrank(bp, wlo, c >> 4) * TS + r];
+        const uint32_t ti = tinfo[wrank(bp, wlo, c >> 4)].y;
+        const uint32_t w = rows[(ti >> 16) + __popc(ti & ((1u << r) - 1u))];
         atomicAdd(&acc[(int)(w >> 16) + __popc((w & 0xffffu) >> (16 - (c & 15)))], e.va * l.vb);
     }
 };
@@ -468,13 +473,13 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     constexpr int ARENA = nw_arena<ACC>();
-    uint32_t* words = smem;                                                    // [ntw][16], then acc[nv]
+    uint2* tinfo = reinterpret_cast<uint2*>(smem);                             // [ntw], then rows, then acc
     int* cur_s = reinterpret_cast<int*>(reinterpret_cast<char*>(smem) + ARENA); // 4 x MAXA_SMEM
     uint2* bp = reinterpret_cast<uint2*>(cur_s + 4 * MAXA_SMEM);               // nwords_b
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
-    __shared__ int s_nt, s_fx;
+    __shared__ int s_nt, s_fx, s_nrow;
     const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
@@ -484,16 +489,30 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
         init_cursors(it, cu, colidxC, a_ci, b_rp, b_ci);
         int t0 = it.rs;
         while (t0 < it.re) {
-            // window [t0, t1): the longest run of tiles whose row words and
-            // values fit the arena (one tile always fits: 64 + 256 values)
+            // window [t0, t1): the longest run of n tiles whose metadata (8 B
+            // a tile, 4 B a non-empty row: at most min(values, 16 a tile)),
+            // values and 16 B of alignment slack fit the arena (one tile
+            // always fits).  fits(n) is monotone: one sample per thread, then
+            // the bracket after the last fitting sample.
             const int64_t v0 = tile_nnzC[t0];
-            const int cap_t = min(ARENA / 64, it.re - t0);
-            if (tid == 0) s_nt = 0;
+            const int cap_t = min(ARENA / 8, it.re - t0);
+            auto fits = [&](int n) {
+                const int64_t nvx = tile_nnzC[t0 + n] - v0;
+                const int64_t rb = nvx < 16 * (int64_t)n ? nvx : 16 * (int64_t)n;
+                return 8 * (int64_t)n + 4 * rb + (int64_t)sizeof(ACC) * nvx + 16 <= ARENA;
+            };
+            const int step = (cap_t + RW_THREADS - 1) / RW_THREADS;
+            if (tid == 0) { s_nt = 0; s_nrow = 0; }
             __syncthreads();
-            int ok = 0;
-            for (int x = tid; x < cap_t; x += RW_THREADS)
-                ok += (64 * (int64_t)(x + 1) + (int64_t)sizeof(ACC) * (tile_nnzC[t0 + x + 1] - v0) <= ARENA) ? 1 : 0;
-            if (ok) atomicAdd(&s_nt, ok);
+            {
+                const int n = (tid + 1) * step;
+                if (n <= cap_t && fits(n)) atomicMax(&s_nt, n);
+            }
+            __syncthreads();
+            const int lo_n = s_nt;  // fits; lo_n + step does not (or passes cap_t)
+            const int hi_n = min(cap_t, lo_n + step - 1);
+            __syncthreads();
+            if (tid < hi_n - lo_n && fits(lo_n + 1 + tid)) atomicMax(&s_nt, lo_n + 1 + tid);
             __syncthreads();
             const int ntw = max(1, s_nt);
             const int t1 = t0 + ntw;
@@ -507,9 +526,12 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             const int jlo = colidxC[t0], jhi = colidxC[t1 - 1];
             const int wlo = jlo >> 5, nwd = (jhi >> 5) - wlo + 1;
             const int limit = (jhi + 1) * TS;
-            ACC* acc = reinterpret_cast<ACC*>(words + ntw * TS);
-            // row words, one thread per tile: 2 x 16 B of masks, 16 B of row
-            // offsets and the tile's value offset, all loads in flight at once
+            uint32_t* rows = reinterpret_cast<uint32_t*>(tinfo + ntw);
+            const int64_t rcap = nv < 16 * (int64_t)ntw ? nv : 16 * (int64_t)ntw;
+            ACC* acc = reinterpret_cast<ACC*>(rows + ((rcap + 3) & ~(int64_t)3));
+            // tile and row words, one thread per tile: 2 x 16 B of masks, 16 B
+            // of row offsets and the tile's value offset, all loads in flight;
+            // the tile's non-empty rows get a block of row words from a counter
             for (int lt = tid; lt < ntw; lt += RW_THREADS) {
                 const int64_t t = (int64_t)t0 + lt;
                 const uint4 m0 = __ldcs(reinterpret_cast<const uint4*>(maskC) + 2 * t);
@@ -518,36 +540,43 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                 const uint32_t vb = (uint32_t)(tile_nnzC[t] - v0);
                 const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
                 const uint32_t pw[4] = {po.x, po.y, po.z, po.w};
-                uint32_t w[16];
+                uint32_t occ = 0;
+#pragma unroll
+                for (int r = 0; r < TS; r++)
+                    if ((mw[r >> 1] >> (16 * (r & 1))) & 0xffffu) occ |= 1u << r;
+                const int rs = occ ? atomicAdd(&s_nrow, __popc(occ)) : 0;
+                tinfo[lt] = make_uint2(vb, ((uint32_t)rs << 16) | occ);
+                int k = rs;
 #pragma unroll
                 for (int r = 0; r < TS; r++) {
                     const uint32_t m16 = (mw[r >> 1] >> (16 * (r & 1))) & 0xffffu;
-                    const uint32_t off = vb + ((pw[r >> 2] >> (8 * (r & 3))) & 0xffu);
-                    w[r] = (off << 16) | m16;
+                    if (m16) rows[k++] = ((vb + ((pw[r >> 2] >> (8 * (r & 3))) & 0xffu)) << 16) | m16;
                 }
-                uint4* dst = reinterpret_cast<uint4*>(words + lt * TS);
-                dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-                dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
-                dst[2] = make_uint4(w[8], w[9], w[10], w[11]);
-                dst[3] = make_uint4(w[12], w[13], w[14], w[15]);
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bp, s_sh);
             walk_window(it, cu, s_rows, limit, b_ci, &s_fx,
-                        NumOp<V, ACC>{bp, wlo, words, acc, a_val, b_val, it.e0});
+                        NumOp<V, ACC>{bp, wlo, tinfo, rows, acc, a_val, b_val, it.e0});
             __syncthreads();
-            // column bytes: one thread per C tile row writes its run (runs of
-            // consecutive rows are adjacent in colC); values leave coalesced
-            for (int x = tid; x < ntw * TS; x += RW_THREADS) {
-                const uint32_t w = words[x];
-                uint32_t m16 = w & 0xffffu;
-                uint8_t* o = colC + v0 + (w >> 16);
-                const uint8_t rb = (uint8_t)((x & 15) << 4);
-                while (m16) {
-                    const int c = __clz(m16) - 16;
-                    __stcs(o++, (uint8_t)(rb | (uint8_t)c));
-                    m16 &= ~(0x8000u >> c);
+            // column bytes: one thread per tile writes its rows' runs (the
+            // tile's bytes are contiguous in colC); values leave coalesced
+            for (int lt = tid; lt < ntw; lt += RW_THREADS) {
+                const uint32_t ti = tinfo[lt].y;
+                uint32_t occ = ti & 0xffffu;
+                int k = (int)(ti >> 16);
+                while (occ) {
+                    const int r = __ffs(occ) - 1;
+                    occ &= occ - 1u;
+                    const uint32_t w = rows[k++];
+                    uint32_t m16 = w & 0xffffu;
+                    uint8_t* o = colC + v0 + (w >> 16);
+                    const uint8_t rb = (uint8_t)(r << 4);
+                    while (m16) {
+                        const int c = __clz(m16) - 16;
+                        __stcs(o++, (uint8_t)(rb | (uint8_t)c));
+                        m16 &= ~(0x8000u >> c);
+                    }
                 }
             }
             for (int x = tid; x < nv; x += RW_THREADS) __stcs(&valC[v0 + x], (V)acc[x]);
