@@ -401,7 +401,8 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                    const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                    const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                    const int* __restrict__ b_ci, uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC,
-                   int* __restrict__ tile_cnt, unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
+                   int64_t* __restrict__ tile_cnt, unsigned long long* ticket, int* __restrict__ cursor_g,
+                   int max_na) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* masks32 = smem;                      // [16][WS] halfwords
     int* cur_s = reinterpret_cast<int*>(masks32 + WS * 8);  // 4 x MAXA_SMEM
@@ -449,7 +450,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                 __stcs(mo, make_uint4(mw[0], mw[1], mw[2], mw[3]));
                 __stcs(mo + 1, make_uint4(mw[4], mw[5], mw[6], mw[7]));
                 __stcs(reinterpret_cast<uint4*>(ptrRowC) + t, make_uint4(pw[0], pw[1], pw[2], pw[3]));
-                __stcs(&tile_cnt[t], tot);
+                __stcs(reinterpret_cast<long long*>(tile_cnt) + t, (long long)tot);
             }
             __syncthreads();
         }
@@ -651,7 +652,7 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
 }
 
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
-                            int* tile_cnt) {
+                            int64_t* tile_cnt) {
     if (C->numtileC == 0) return SPG_OK;
     SPG_TRY(rw_prepare(h, A, B, C, rp));
     h->stats.work_items = rp->nitems;

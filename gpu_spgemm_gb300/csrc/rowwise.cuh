@@ -14,7 +14,7 @@ struct RowwisePriv {
 
 spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B);
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                            RowwisePriv* rp, int* tile_cnt);
+                            RowwisePriv* rp, int64_t* tile_cnt);
 spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                            RowwisePriv* rp, spg_precision prec);
 void rowwise_free_priv(spg_handle_t h, RowwisePriv* rp);

@@ -21,6 +21,7 @@ struct CPriv {
     int64_t* row_pairs = nullptr;  // tilem: tile pairs per C tile-row (step 1)
     spg_algo algo = SPG_ALGO_PLAIN;
     RowwisePriv rw;
+    bool vals_joint = false;       // tile_colC lives inside tile_valC's allocation
 };
 
 RowwisePriv* ctiles_rowwise_priv(spg_ctiles* C) {
@@ -226,8 +227,9 @@ static float elapsed(spg_handle_t h, int a, int b) {
 
 extern "C" spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C) {
     if (!h || !C) return SPG_ERR_INVALID;
+    const bool joint = C->priv && static_cast<CPriv*>(C->priv)->vals_joint;
     void* ptrs[] = {C->tile_ptrC, C->tile_rowidxC, C->tile_colidxC, C->maskC, C->tile_nnzC, C->ptrRowC,
-                    C->tile_valC, C->tile_colC};
+                    C->tile_valC, joint ? nullptr : C->tile_colC};
     for (void* p : ptrs) spg_free_async(h, p);
     if (C->priv) {
         CPriv* cp = static_cast<CPriv*>(C->priv);
@@ -273,10 +275,12 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
     SPG_TRY(spg_alloc_t(h, &C->maskC, (size_t)nt * TS + 16));
     SPG_TRY(spg_alloc_t(h, &C->ptrRowC, (size_t)nt * TS + 16));
     SPG_TRY(spg_alloc_t(h, &C->tile_nnzC, (size_t)nt + 1));
-    SPG_TRY(spg_alloc_t(h, &tile_cnt, (size_t)nt + 1));
     if (algo == SPG_ALGO_ROWWISE) {
-        SPG_TRY(rowwise_symbolic(h, A, B, C, &cp->rw, tile_cnt));
+        // tile counts land in tile_nnzC itself and are scanned in place
+        SPG_TRY(rowwise_symbolic(h, A, B, C, &cp->rw, C->tile_nnzC));
+        SPG_TRY(spg_scan_i64_to_i64(h, C->tile_nnzC, C->tile_nnzC, nt));
     } else {
+        SPG_TRY(spg_alloc_t(h, &tile_cnt, (size_t)nt + 1));
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
         int64_t cap = 8 * nt;  // src/spgemm_raw_v2.cu:170
@@ -292,9 +296,9 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_pb, (size_t)cap + 1));
         }
         SPG_TRY(plain_step2(h, A, B, C, &cp->plain, tile_cnt));
+        SPG_TRY(spg_scan_i32_to_i64(h, tile_cnt, C->tile_nnzC, nt));
+        spg_free_async(h, tile_cnt);
     }
-    SPG_TRY(spg_scan_i32_to_i64(h, tile_cnt, C->tile_nnzC, nt));
-    spg_free_async(h, tile_cnt);
     SPG_TRY(spg_read_i64(h, C->tile_nnzC + nt, &C->nnzC));
     {
         int64_t pairs = 0;
@@ -302,8 +306,13 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
         C->pairs = pairs;
     }
     const size_t vs = val_size(C->dtype);
-    SPG_TRY(spg_alloc(h, &C->tile_valC, vs * ((size_t)C->nnzC + 1)));
-    SPG_TRY(spg_alloc_t(h, &C->tile_colC, (size_t)C->nnzC + 16));
+    {   // values and column bytes in one allocation: a repeated product of the
+        // same size then reuses one pooled block instead of splitting others
+        const size_t vbytes = (vs * ((size_t)C->nnzC + 1) + 255) & ~(size_t)255;
+        SPG_TRY(spg_alloc(h, &C->tile_valC, vbytes + (size_t)C->nnzC + 16));
+        C->tile_colC = static_cast<uint8_t*>(C->tile_valC) + vbytes;
+        cp->vals_joint = true;
+    }
     SPG_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
     SPG_CUDA(h, cudaEventSynchronize(h->ev[2]));
     h->stats.ms_step1 = elapsed(h, 0, 1);
