@@ -433,24 +433,38 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             build_window_rank(colidxC, w0, nt, wlo, nwd, bp, s_sh);
             walk_window(it, cu, s_rows, limit, b_ci, &s_fx, SymOp{bp, wlo, masks32});
             __syncthreads();
-            for (int x = tid; x < nt; x += RW_THREADS) {
-                uint32_t mw[8];
-                uint32_t pw[4] = {0u, 0u, 0u, 0u};
+            // write-out: lane pair (2j, 2j+1) takes one tile, each lane 8 of its
+            // rows, so a warp's stores cover 16 tiles' contiguous masks (512 B)
+            // and row offsets (256 B); the low half's count reaches the high
+            // half by shuffle
+            for (int q0 = 0; q0 < 2 * nt; q0 += RW_THREADS) {
+                const int q = q0 + tid;
+                const bool act = q < 2 * nt;
+                const int x = q >> 1, hh = q & 1;
+                uint32_t mw[4] = {0u, 0u, 0u, 0u};
+                uint32_t pw[2] = {0u, 0u};
                 int tot = 0;
+                if (act) {
 #pragma unroll
-                for (int r = 0; r < TS; r++) {
-                    const int idx = r * WS + x;
-                    const uint32_t m16 = (masks32[idx >> 1] >> ((idx & 1) * 16)) & 0xffffu;
-                    if (r & 1) mw[r >> 1] |= m16 << 16; else mw[r >> 1] = m16;
-                    pw[r >> 2] |= (uint32_t)(tot & 0xff) << (8 * (r & 3));
-                    tot += __popc(m16);
+                    for (int r8 = 0; r8 < 8; r8++) {
+                        const int idx = (8 * hh + r8) * WS + x;
+                        const uint32_t m16 = (masks32[idx >> 1] >> ((idx & 1) * 16)) & 0xffffu;
+                        mw[r8 >> 1] |= m16 << (16 * (r8 & 1));
+                        pw[r8 >> 2] |= (uint32_t)tot << (8 * (r8 & 3));
+                        tot += __popc(m16);
+                    }
                 }
-                const int64_t t = (int64_t)w0 + x;
-                uint4* mo = reinterpret_cast<uint4*>(maskC) + 2 * t;
-                __stcs(mo, make_uint4(mw[0], mw[1], mw[2], mw[3]));
-                __stcs(mo + 1, make_uint4(mw[4], mw[5], mw[6], mw[7]));
-                __stcs(reinterpret_cast<uint4*>(ptrRowC) + t, make_uint4(pw[0], pw[1], pw[2], pw[3]));
-                __stcs(reinterpret_cast<long long*>(tile_cnt) + t, (long long)tot);
+                const int low = __shfl_xor_sync(0xffffffffu, tot, 1);  // the pair's other half
+                if (act) {
+                    const int64_t t = (int64_t)w0 + x;
+                    if (hh) {  // rows 8..15 start after rows 0..7 (every byte stays <= 240)
+                        pw[0] += (uint32_t)low * 0x01010101u;
+                        pw[1] += (uint32_t)low * 0x01010101u;
+                        __stcs(reinterpret_cast<long long*>(tile_cnt) + t, (long long)(low + tot));
+                    }
+                    __stcs(reinterpret_cast<uint4*>(maskC) + 2 * t + hh, make_uint4(mw[0], mw[1], mw[2], mw[3]));
+                    __stcs(reinterpret_cast<uint2*>(ptrRowC) + 2 * t + hh, make_uint2(pw[0], pw[1]));
+                }
             }
             __syncthreads();
         }
