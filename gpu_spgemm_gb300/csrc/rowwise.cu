@@ -35,7 +35,7 @@ constexpr int RW_THREADS = 512;
 constexpr int RW_WARPS = RW_THREADS / 32;
 constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
-// numeric window arena (bytes): 8 B a tile + 4 B a non-empty tile row +
+// numeric window arena (bytes): 8 B a tile + 5 B a non-empty tile row +
 // sizeof(ACC) a value
 constexpr int NW_ARENA_F32 = 74752;   // two blocks per SM
 constexpr int NW_ARENA_F64 = 131072;  // one block per SM
@@ -505,7 +505,7 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
         int t0 = it.rs;
         while (t0 < it.re) {
             // window [t0, t1): the longest run of n tiles whose metadata (8 B
-            // a tile, 4 B a non-empty row: at most min(values, 16 a tile)),
+            // a tile, 5 B a non-empty row: at most min(values, 16 a tile)),
             // values and 16 B of alignment slack fit the arena (one tile
             // always fits).  fits(n) is monotone: one sample per thread, then
             // the bracket after the last fitting sample.
@@ -514,7 +514,7 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             auto fits = [&](int n) {
                 const int64_t nvx = tile_nnzC[t0 + n] - v0;
                 const int64_t rb = nvx < 16 * (int64_t)n ? nvx : 16 * (int64_t)n;
-                return 8 * (int64_t)n + 4 * rb + (int64_t)sizeof(ACC) * nvx + 16 <= ARENA;
+                return 8 * (int64_t)n + 5 * rb + (int64_t)sizeof(ACC) * nvx + 16 <= ARENA;
             };
             const int step = (cap_t + RW_THREADS - 1) / RW_THREADS;
             if (tid == 0) { s_nt = 0; s_nrow = 0; }
@@ -543,7 +543,9 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             const int limit = (jhi + 1) * TS;
             uint32_t* rows = reinterpret_cast<uint32_t*>(tinfo + ntw);
             const int64_t rcap = nv < 16 * (int64_t)ntw ? nv : 16 * (int64_t)ntw;
-            ACC* acc = reinterpret_cast<ACC*>(rows + ((rcap + 3) & ~(int64_t)3));
+            uint8_t* rowr = reinterpret_cast<uint8_t*>(rows + rcap);  // each row word's row in its tile
+            const size_t aoff = ((size_t)(rowr + rcap - reinterpret_cast<uint8_t*>(smem)) + 15) & ~(size_t)15;
+            ACC* acc = reinterpret_cast<ACC*>(reinterpret_cast<uint8_t*>(smem) + aoff);  // 16-byte aligned
             // tile and row words, one thread per tile: 2 x 16 B of masks, 16 B
             // of row offsets and the tile's value offset, all loads in flight;
             // the tile's non-empty rows get a block of row words from a counter
@@ -565,7 +567,10 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
 #pragma unroll
                 for (int r = 0; r < TS; r++) {
                     const uint32_t m16 = (mw[r >> 1] >> (16 * (r & 1))) & 0xffffu;
-                    if (m16) rows[k++] = ((vb + ((pw[r >> 2] >> (8 * (r & 3))) & 0xffu)) << 16) | m16;
+                    if (m16) {
+                        rowr[k] = (uint8_t)r;
+                        rows[k++] = ((vb + ((pw[r >> 2] >> (8 * (r & 3))) & 0xffu)) << 16) | m16;
+                    }
                 }
             }
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
@@ -574,24 +579,18 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             walk_window(it, cu, s_rows, limit, b_ci, &s_fx,
                         NumOp<V, ACC>{bp, wlo, tinfo, rows, acc, a_val, b_val, it.e0});
             __syncthreads();
-            // column bytes: one thread per tile writes its rows' runs (the
-            // tile's bytes are contiguous in colC); values leave coalesced
-            for (int lt = tid; lt < ntw; lt += RW_THREADS) {
-                const uint32_t ti = tinfo[lt].y;
-                uint32_t occ = ti & 0xffffu;
-                int k = (int)(ti >> 16);
-                while (occ) {
-                    const int r = __ffs(occ) - 1;
-                    occ &= occ - 1u;
-                    const uint32_t w = rows[k++];
-                    uint32_t m16 = w & 0xffffu;
-                    uint8_t* o = colC + v0 + (w >> 16);
-                    const uint8_t rb = (uint8_t)(r << 4);
-                    while (m16) {
-                        const int c = __clz(m16) - 16;
-                        __stcs(o++, (uint8_t)(rb | (uint8_t)c));
-                        m16 &= ~(0x8000u >> c);
-                    }
+            // column bytes: one thread per non-empty tile row writes its run;
+            // values leave coalesced
+            const int nrow = s_nrow;
+            for (int k = tid; k < nrow; k += RW_THREADS) {
+                const uint32_t w = rows[k];
+                uint32_t m16 = w & 0xffffu;
+                uint8_t* o = colC + v0 + (w >> 16);
+                const uint8_t rb = (uint8_t)(rowr[k] << 4);
+                while (m16) {
+                    const int c = __clz(m16) - 16;
+                    __stcs(o++, (uint8_t)(rb | (uint8_t)c));
+                    m16 &= ~(0x8000u >> c);
                 }
             }
             for (int x = tid; x < nv; x += RW_THREADS) __stcs(&valC[v0 + x], (V)acc[x]);
