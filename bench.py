@@ -224,6 +224,7 @@ def run_ours(args):
     B = api.build_csc_tiles(h, b)
     products = api.products(h, A, B)
     flops = 2.0 * products
+    h.set_mixed_params(args.dense_thr)
     sizing = None
     if args.sizing and os.path.exists(api.SIZING_MODEL_PATH):
         sizing = api.SizingModel.load(h)
@@ -606,6 +607,8 @@ def main():
     p.add_argument("--sizing", type=int, default=1, help="attach the trained sizing MLP (1) or not (0)")
     p.add_argument("--sizing-margin", type=float, default=1.0,
                    help="slot of a tile-row = predicted tiles * (1 + margin) + 2")
+    p.add_argument("--dense-thr", type=int, default=32,
+                   help="--prec mixed: tile pairs with both tiles >= this many nonzeros go to tensor cores")
     p.add_argument("--traffic", type=float, default=None,
                    help="dram bytes per launch of the dominant kernel from an ncu capture")
     args = p.parse_args()

@@ -58,6 +58,11 @@ class Handle:
         s = getattr(stream, "cuda_stream", stream)
         self.check(self.lib.spg_set_stream(self.h, C.c_void_p(s or 0)))
 
+    def set_mixed_params(self, dense_thr: int = 32, cancel_eps: float = 2.0 ** -20):
+        """SPG_PREC_MIXED: tensor-core threshold (nonzeros in both tiles) and
+        the cancellation bound that sends a C tile to FP64."""
+        self.check(self.lib.spg_set_mixed_params(self.h, int(dense_thr), float(cancel_eps)))
+
     def stats(self) -> dict:
         st = L.SpgStats()
         self.check(self.lib.spg_get_stats(self.h, C.byref(st)))

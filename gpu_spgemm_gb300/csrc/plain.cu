@@ -139,7 +139,6 @@ c1_slot_kernel(const int* __restrict__ a_tp, const int* __restrict__ a_tc, const
     extern __shared__ uint32_t bm[];
     __shared__ int s_span[4];
     __shared__ int64_t s_sh[C1_WARPS + 1];
-    __shared__ int s_c[C1_WARPS];
     __shared__ int64_t s_p[C1_WARPS];
     const int i = blockIdx.x;
     if (a_tp[i] == a_tp[i + 1]) {
@@ -157,7 +156,6 @@ c1_slot_kernel(const int* __restrict__ a_tp, const int* __restrict__ a_tc, const
     pairs = warp_sum(pairs);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) s_p[warp] = pairs;
-    (void)s_c;
     __syncthreads();
     if (threadIdx.x == 0) {
         int64_t p = 0;
@@ -306,7 +304,7 @@ c2_symbolic_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int*
 // keep 16 register accumulators; B's row is walked through its 16-bit mask
 // with predicated FMAs instead of the reference's 16-way switch; a shuffle
 // combines the halves and half 0 compacts the row by maskC.
-template <typename V, bool CACHE>
+template <typename V, bool CACHE, bool SKIP_DENSE = false>
 __global__ void __launch_bounds__(256)
 c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
                   const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ a_tnnz,
@@ -318,7 +316,8 @@ c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* 
                   const uint16_t* __restrict__ maskC, const uint8_t* __restrict__ ptrRowC,
                   V* __restrict__ valC, uint8_t* __restrict__ colC, const int* __restrict__ spec_cnt,
                   const int* __restrict__ spec_off, const int* __restrict__ spec_pa,
-                  const int* __restrict__ spec_pb) {
+                  const int* __restrict__ spec_pb, int dense_thr = 0, int* __restrict__ dense_tiles = nullptr,
+                  unsigned* __restrict__ n_dense_tiles = nullptr) {
     const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < numtileC; t += nwarps) {
@@ -327,8 +326,13 @@ c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* 
         V acc[TS];
 #pragma unroll
         for (int c = 0; c < TS; c++) acc[c] = V(0);
+        bool skipped = false;  // warp-uniform: a dense pair was left to the tensor kernel
         auto do_pair = [&](int pa, int pb) {
             const int sA = __ldg(&a_tnnz[pa]), na = __ldg(&a_tnnz[pa + 1]) - sA;
+            if (SKIP_DENSE && na >= dense_thr && __ldg(&b_tnnz[pb + 1]) - __ldg(&b_tnnz[pb]) >= dense_thr) {
+                skipped = true;
+                return;
+            }
             const int rs = __ldg(&a_ptr16[(int64_t)pa * TS + r]);
             const int re = (r == TS - 1) ? na : (int)__ldg(&a_ptr16[(int64_t)pa * TS + r + 1]);
             const int sB = __ldg(&b_tnnz[pb]);
@@ -391,23 +395,25 @@ c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* 
                 }
             }
         }
+        if (SKIP_DENSE && skipped && lane == 0) dense_tiles[atomicAdd(n_dense_tiles, 1u)] = (int)t;
     }
 }
 
 // ---------------------------------------------------------------------------
-// Mixed precision (SPG_PREC_MIXED, FP32 data): the per-C-tile kernel above,
-// with every matched tile pair whose A and B tiles both hold >= dense_thr
-// nonzeros computed as a real 16x16x16 contraction on the tensor cores:
-// mma.sync m16n8k16, FP16 operands, FP32 accumulation, each FP32 value split
-// x = hi + lo (hi = fp16(x), lo = fp16(x - hi)) and hi*hi + hi*lo + lo*hi
-// accumulated (the dropped lo*lo term is ~2^-22 relative).  tcgen05.mma needs
-// M >= 64; one 16x16 tile pair fills a single m16n8k16 pair exactly, and
-// stacking tile pairs to M = 64/128 would multiply mostly zero padding on
-// these sparse tile rows.  Each lane builds its fragments straight from the
-// compressed tile (16-bit row masks + popc offsets): no shared-memory
-// densification.  A |A|*|B| magnitude product (hi parts) flags C tiles whose
-// entries cancelled to below cancel_eps of their magnitude; those tiles are
-// recomputed in FP64 by c3_fp64_list_kernel.
+// Mixed precision (SPG_PREC_MIXED, FP32 data): every matched tile pair whose
+// A and B tiles both hold >= dense_thr nonzeros is computed as a real
+// 16x16x16 contraction on the tensor cores: mma.sync m16n8k16, FP16 operands,
+// FP32 accumulation, each FP32 value split x = hi + lo (hi = fp16(x), lo =
+// fp16(x - hi)) and hi*hi + hi*lo + lo*hi accumulated (the dropped lo*lo term
+// is ~2^-22 relative).  tcgen05.mma needs M >= 64; one 16x16 tile pair fills
+// a single m16n8k16 pair exactly, and stacking tile pairs to M = 64/128 would
+// multiply mostly zero padding on these tile rows.  Two kernels: the plain
+// register kernel writes every C tile from its sparse pairs (dense pairs
+// skipped, tiles that had one listed), then the tensor kernel adds the listed
+// tiles' dense pairs from fragments built once per dense tile.  A |A|*|B|
+// magnitude product (hi parts) flags C tiles whose entries cancelled to below
+// cancel_eps of their magnitude; those tiles are recomputed in FP64 by
+// c3_fp64_list_kernel.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
     asm volatile(
@@ -434,91 +440,110 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_
     ab = *reinterpret_cast<const uint32_t*>(&A);
 }
 
+// Dense tiles (>= dense_thr nonzeros) in mma.sync fragment form, built once
+// per product: per tile and lane 12 words, read back with three coalesced
+// 16-byte loads per pair instead of rebuilding the fragment from the
+// compressed tile for every pair.
+//   A (row operand, m16 x k16): ah[4], al[4], |a|[4] for rows g, g+8 and
+//     columns 2q, 2q+1, 2q+8, 2q+9 (g = lane/4, q = lane%4);
+//   B (column operand, k16 x n16): for n halves h = 0, 1: bh[2], bl[2], |b|[2]
+//     for rows 2q, 2q+1, 2q+8, 2q+9 and column g + 8h.
+__global__ void dense_flag_kernel(int64_t numtile, const int* __restrict__ tnnz, int dense_thr, int* __restrict__ flag) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < numtile; t += (int64_t)gridDim.x * blockDim.x)
+        flag[t] = (tnnz[t + 1] - tnnz[t] >= dense_thr) ? 1 : 0;
+}
+
+template <bool IS_B>
+__global__ void __launch_bounds__(256)
+dense_frag_kernel(int64_t numtile, const int* __restrict__ tnnz, const float* __restrict__ val,
+                  const uint8_t* __restrict__ ptr16, const uint16_t* __restrict__ mask, int dense_thr,
+                  const int* __restrict__ slot, uint4* __restrict__ frag) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < numtile; t += nw) {
+        const int s0 = tnnz[t];
+        if (tnnz[t + 1] - s0 < dense_thr) continue;
+        uint32_t w[12];
+        if (!IS_B) {
+            const uint32_t m0 = mask[t * TS + g], m1 = mask[t * TS + g + 8];
+            const int p0 = ptr16[t * TS + g], p1 = ptr16[t * TS + g + 8];
+            const int c0 = 2 * tq;
+            split2(tile_elem(val, s0, m0, p0, c0), tile_elem(val, s0, m0, p0, c0 + 1), w[0], w[4], w[8]);
+            split2(tile_elem(val, s0, m1, p1, c0), tile_elem(val, s0, m1, p1, c0 + 1), w[1], w[5], w[9]);
+            split2(tile_elem(val, s0, m0, p0, c0 + 8), tile_elem(val, s0, m0, p0, c0 + 9), w[2], w[6], w[10]);
+            split2(tile_elem(val, s0, m1, p1, c0 + 8), tile_elem(val, s0, m1, p1, c0 + 9), w[3], w[7], w[11]);
+        } else {
+            const int k0 = 2 * tq;
+            const uint32_t bm0 = mask[t * TS + k0], bm1 = mask[t * TS + k0 + 1];
+            const uint32_t bm2 = mask[t * TS + k0 + 8], bm3 = mask[t * TS + k0 + 9];
+            const int bp0 = ptr16[t * TS + k0], bp1 = ptr16[t * TS + k0 + 1];
+            const int bp2 = ptr16[t * TS + k0 + 8], bp3 = ptr16[t * TS + k0 + 9];
+#pragma unroll
+            for (int nh = 0; nh < 2; nh++) {
+                const int n = g + 8 * nh;
+                split2(tile_elem(val, s0, bm0, bp0, n), tile_elem(val, s0, bm1, bp1, n), w[6 * nh + 0], w[6 * nh + 2],
+                       w[6 * nh + 4]);
+                split2(tile_elem(val, s0, bm2, bp2, n), tile_elem(val, s0, bm3, bp3, n), w[6 * nh + 1], w[6 * nh + 3],
+                       w[6 * nh + 5]);
+            }
+        }
+        uint4* dst = frag + ((int64_t)slot[t] * 32 + lane) * 3;
+        dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+        dst[2] = make_uint4(w[8], w[9], w[10], w[11]);
+    }
+}
+
+// Tensor part of SPG_PREC_MIXED, run after the register kernel has written
+// every C tile from its sparse pairs: one warp per listed C tile (those with a
+// pair of dense tiles) accumulates the dense pairs with mma.sync from the
+// precomputed fragments (hi*hi + hi*lo + lo*hi, and |a|*|b| for the
+// cancellation test), adds them to the tile's values and lists the tile for
+// FP64 recomputation if an entry cancelled below cancel_eps of its magnitude.
 template <bool CACHE>
 __global__ void __launch_bounds__(256)
-c3_mixed_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
-                const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ a_tnnz,
-                const float* __restrict__ a_val, const uint8_t* __restrict__ a_col, const uint8_t* __restrict__ a_ptr16,
-                const uint16_t* __restrict__ a_mask, const int* __restrict__ b_cscp, const int* __restrict__ b_cscr,
-                const int* __restrict__ b_tnnz, const float* __restrict__ b_val, const uint8_t* __restrict__ b_ptr16,
-                const uint16_t* __restrict__ b_mask, const int64_t* __restrict__ tile_nnzC,
-                const uint16_t* __restrict__ maskC, const uint8_t* __restrict__ ptrRowC, float* __restrict__ valC,
-                uint8_t* __restrict__ colC, const int* __restrict__ spec_cnt, const int* __restrict__ spec_off,
-                const int* __restrict__ spec_pa, const int* __restrict__ spec_pb, int dense_thr, float cancel_eps,
-                unsigned long long* __restrict__ tensor_pairs, int* __restrict__ flag_list,
-                unsigned* __restrict__ nflag) {
+c3_tensor_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ rowidxC,
+                 const int* __restrict__ colidxC, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
+                 const int* __restrict__ a_tnnz, const int* __restrict__ b_cscp, const int* __restrict__ b_cscr,
+                 const int* __restrict__ b_tnnz, const int64_t* __restrict__ tile_nnzC,
+                 const uint16_t* __restrict__ maskC, const uint8_t* __restrict__ ptrRowC, float* __restrict__ valC,
+                 const int* __restrict__ spec_cnt, const int* __restrict__ spec_off, const int* __restrict__ spec_pa,
+                 const int* __restrict__ spec_pb, int dense_thr, float cancel_eps,
+                 unsigned long long* __restrict__ tensor_pairs, int* __restrict__ flag_list,
+                 unsigned* __restrict__ nflag, const uint4* __restrict__ fragA, const int* __restrict__ slotA,
+                 const uint4* __restrict__ fragB, const int* __restrict__ slotB) {
     __shared__ float s_tile[8][TS][TS + 1];
     __shared__ float s_mag[8][TS][TS + 1];
     const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
     const int g = lane >> 2, tq = lane & 3;
     const int wib = threadIdx.x >> 5;
     unsigned long long my_tensor = 0;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib; t < numtileC; t += nwarps) {
-        const int64_t cbase = tile_nnzC[t];
-        if (tile_nnzC[t + 1] == cbase) continue;
-        float acc[TS];
-#pragma unroll
-        for (int c = 0; c < TS; c++) acc[c] = 0.f;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + wib; w < ntiles; w += nwarps) {
+        const int64_t t = tiles[w];
         float d[8], mg[8];
 #pragma unroll
         for (int q = 0; q < 8; q++) { d[q] = 0.f; mg[q] = 0.f; }
         auto do_pair = [&](int pa, int pb) {
-            const int sA = __ldg(&a_tnnz[pa]), na = __ldg(&a_tnnz[pa + 1]) - sA;
-            const int sB = __ldg(&b_tnnz[pb]), nb = __ldg(&b_tnnz[pb + 1]) - sB;
-            if (na >= dense_thr && nb >= dense_thr) {  // warp-uniform: tensor-core pair
-                __syncwarp();  // mma.sync.aligned: the whole warp converged
-                if (lane == 0) my_tensor++;
-                uint32_t ah[4], al[4], aa[4];
-                {
-                    const uint32_t m0 = __ldg(&a_mask[(int64_t)pa * TS + g]);
-                    const uint32_t m1 = __ldg(&a_mask[(int64_t)pa * TS + g + 8]);
-                    const int p0 = __ldg(&a_ptr16[(int64_t)pa * TS + g]);
-                    const int p1 = __ldg(&a_ptr16[(int64_t)pa * TS + g + 8]);
-                    const int c0 = 2 * tq;
-                    split2(tile_elem(a_val, sA, m0, p0, c0), tile_elem(a_val, sA, m0, p0, c0 + 1), ah[0], al[0], aa[0]);
-                    split2(tile_elem(a_val, sA, m1, p1, c0), tile_elem(a_val, sA, m1, p1, c0 + 1), ah[1], al[1], aa[1]);
-                    split2(tile_elem(a_val, sA, m0, p0, c0 + 8), tile_elem(a_val, sA, m0, p0, c0 + 9), ah[2], al[2],
-                           aa[2]);
-                    split2(tile_elem(a_val, sA, m1, p1, c0 + 8), tile_elem(a_val, sA, m1, p1, c0 + 9), ah[3], al[3],
-                           aa[3]);
-                }
-                const int k0 = 2 * tq;
-                const uint32_t bm0 = __ldg(&b_mask[(int64_t)pb * TS + k0]);
-                const uint32_t bm1 = __ldg(&b_mask[(int64_t)pb * TS + k0 + 1]);
-                const uint32_t bm2 = __ldg(&b_mask[(int64_t)pb * TS + k0 + 8]);
-                const uint32_t bm3 = __ldg(&b_mask[(int64_t)pb * TS + k0 + 9]);
-                const int bp0 = __ldg(&b_ptr16[(int64_t)pb * TS + k0]);
-                const int bp1 = __ldg(&b_ptr16[(int64_t)pb * TS + k0 + 1]);
-                const int bp2 = __ldg(&b_ptr16[(int64_t)pb * TS + k0 + 8]);
-                const int bp3 = __ldg(&b_ptr16[(int64_t)pb * TS + k0 + 9]);
-#pragma unroll
-                for (int nh = 0; nh < 2; nh++) {
-                    const int n = g + 8 * nh;
-                    uint32_t bh[2], bl[2], ba[2];
-                    split2(tile_elem(b_val, sB, bm0, bp0, n), tile_elem(b_val, sB, bm1, bp1, n), bh[0], bl[0], ba[0]);
-                    split2(tile_elem(b_val, sB, bm2, bp2, n), tile_elem(b_val, sB, bm3, bp3, n), bh[1], bl[1], ba[1]);
-                    mma16816(d + 4 * nh, ah, bh);
-                    mma16816(d + 4 * nh, ah, bl);
-                    mma16816(d + 4 * nh, al, bh);
-                    mma16816(mg + 4 * nh, aa, ba);
-                }
+            if (__ldg(&a_tnnz[pa + 1]) - __ldg(&a_tnnz[pa]) < dense_thr ||
+                __ldg(&b_tnnz[pb + 1]) - __ldg(&b_tnnz[pb]) < dense_thr)
                 return;
-            }
-            const int rs = __ldg(&a_ptr16[(int64_t)pa * TS + r]);
-            const int re = (r == TS - 1) ? na : (int)__ldg(&a_ptr16[(int64_t)pa * TS + r + 1]);
-            for (int e = rs + hsel; e < re; e += 2) {
-                const int kk = __ldg(&a_col[sA + e]) & 15;
-                const float va = __ldg(&a_val[sA + e]);
-                const uint32_t mb = __ldg(&b_mask[(int64_t)pb * TS + kk]);
-                int off = sB + __ldg(&b_ptr16[(int64_t)pb * TS + kk]);
+            __syncwarp();  // mma.sync.aligned: the whole warp converged
+            if (lane == 0) my_tensor++;
+            const uint4* fa = fragA + ((int64_t)__ldg(&slotA[pa]) * 32 + lane) * 3;
+            const uint4* fb = fragB + ((int64_t)__ldg(&slotB[pb]) * 32 + lane) * 3;
+            const uint4 a0 = __ldg(fa), a1 = __ldg(fa + 1), a2 = __ldg(fa + 2);
+            const uint4 b0 = __ldg(fb), b1 = __ldg(fb + 1), b2 = __ldg(fb + 2);
+            const uint32_t ah[4] = {a0.x, a0.y, a0.z, a0.w}, al[4] = {a1.x, a1.y, a1.z, a1.w};
+            const uint32_t aa[4] = {a2.x, a2.y, a2.z, a2.w};
+            const uint32_t bw[12] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w};
 #pragma unroll
-                for (int c = 0; c < TS; c++) {
-                    if (mb & (0x8000u >> c)) {
-                        acc[c] = fmaf(va, __ldg(&b_val[off]), acc[c]);
-                        off++;
-                    }
-                }
+            for (int nh = 0; nh < 2; nh++) {
+                const uint32_t* bb = bw + 6 * nh;  // bh[2], bl[2], |b|[2]
+                mma16816(d + 4 * nh, ah, bb);
+                mma16816(d + 4 * nh, ah, bb + 2);
+                mma16816(d + 4 * nh, al, bb);
+                mma16816(mg + 4 * nh, aa, bb + 4);
             }
         };
         int cnt = CACHE ? spec_cnt[t] : -1;
@@ -552,7 +577,6 @@ c3_mixed_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __
                 }
             }
         }
-        // combine tensor fragments and register accumulators in shared memory
 #pragma unroll
         for (int nh = 0; nh < 2; nh++) {
             const int c = 2 * tq + 8 * nh;
@@ -565,21 +589,18 @@ c3_mixed_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __
             s_mag[wib][g + 8][c] = mg[4 * nh + 2];
             s_mag[wib][g + 8][c + 1] = mg[4 * nh + 3];
         }
-#pragma unroll
-        for (int c = 0; c < TS; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
         __syncwarp();
         int flagged = 0;
         if (hsel == 0) {
             const uint32_t mc = maskC[t * TS + r];
-            int64_t p = cbase + ptrRowC[t * TS + r];
+            int64_t p = tile_nnzC[t] + ptrRowC[t * TS + r];
 #pragma unroll
             for (int c = 0; c < TS; c++) {
                 if (mc & (0x8000u >> c)) {
-                    const float v = acc[c] + s_tile[wib][r][c];
+                    const float v = valC[p] + s_tile[wib][r][c];
                     const float mag = s_mag[wib][r][c];
                     if (mag > 0.f && fabsf(v) < cancel_eps * mag) flagged = 1;
                     valC[p] = v;
-                    colC[p] = (uint8_t)((r << 4) | c);
                     p++;
                 }
             }
@@ -852,25 +873,77 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
     if (A->dtype != SPG_F32) return spg_fail(h, SPG_ERR_INVALID, "mixed precision needs FP32 data");
     unsigned long long* ctr = nullptr;
     int* list = nullptr;
-    SPG_TRY(spg_alloc_t(h, &ctr, 2));
+    SPG_TRY(spg_alloc_t(h, &ctr, 2));  // [0] tensor pairs, [1] low word: flagged tiles, high word: dense tiles
     SPG_TRY(spg_alloc_t(h, &list, (size_t)nt + 1));
     SPG_CUDA(h, cudaMemsetAsync(ctr, 0, 16, h->stream));
+    // dense tiles of A (row order) and B (CSC order) into fragment form
+    int *slotA = nullptr, *slotB = nullptr;
+    uint4 *fragA = nullptr, *fragB = nullptr;
+    auto build = [&](const spg_tiles* T, bool is_b, int** slot, uint4** frag) -> spg_status {
+        const int64_t n = T->numtile;
+        SPG_TRY(spg_alloc_t(h, slot, (size_t)n + 1));
+        if (n > 0) {
+            dense_flag_kernel<<<grid_cap(h, n, 256, 8), 256, 0, h->stream>>>(n, T->tile_nnz, dense_thr, *slot);
+            SPG_CUDA(h, cudaGetLastError());
+        }
+        SPG_TRY(spg_scan_i32_to_i32(h, *slot, *slot, n));
+        int nd = 0;
+        SPG_TRY(spg_read_i32(h, *slot + n, &nd));
+        SPG_TRY(spg_alloc_t(h, frag, (size_t)nd * 32 * 3 + 1));
+        if (nd > 0) {
+            if (is_b)
+                dense_frag_kernel<true><<<grid_cap(h, n * 32, 256, 16), 256, 0, h->stream>>>(
+                    n, T->tile_nnz, (const float*)T->tile_csr_Val, T->tile_csr_Ptr, T->mask, dense_thr, *slot, *frag);
+            else
+                dense_frag_kernel<false><<<grid_cap(h, n * 32, 256, 16), 256, 0, h->stream>>>(
+                    n, T->tile_nnz, (const float*)T->tile_csr_Val, T->tile_csr_Ptr, T->mask, dense_thr, *slot, *frag);
+            SPG_CUDA(h, cudaGetLastError());
+        }
+        return SPG_OK;
+    };
+    SPG_TRY(build(A, false, &slotA, &fragA));
+    SPG_TRY(build(B, true, &slotB, &fragB));
     const int grid = grid_cap(h, nt, 8, 32);
     const bool cache = pp && pp->spec_cap > 0;
-#define MIXED_ARGS                                                                                                  \
+    // 1. every C tile from its sparse pairs on FP32 registers (the plain
+    //    kernel, dense pairs skipped); tiles with a dense pair are listed
+    int* dense_tiles = nullptr;
+    unsigned* n_dense = reinterpret_cast<unsigned*>(ctr) + 3;  // high word of ctr[1]
+    SPG_TRY(spg_alloc_t(h, &dense_tiles, (size_t)nt + 1));
+#define REG_ARGS                                                                                                    \
     nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const float*)A->tile_csr_Val, \
-        A->tile_csr_Col, A->tile_csr_Ptr, A->mask, B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz,               \
+        A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz,                        \
         (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,                \
         (float*)C->tile_valC, C->tile_colC
     if (cache)
-        c3_mixed_kernel<true><<<grid, 256, 0, h->stream>>>(MIXED_ARGS, pp->spec_cnt, pp->spec_off, pp->spec_pa,
-                                                            pp->spec_pb, dense_thr, cancel_eps, ctr,
-                                                            list, reinterpret_cast<unsigned*>(ctr + 1));
+        c3_numeric_kernel<float, true, true><<<grid, 256, 0, h->stream>>>(
+            REG_ARGS, pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb, dense_thr, dense_tiles, n_dense);
     else
-        c3_mixed_kernel<false><<<grid, 256, 0, h->stream>>>(MIXED_ARGS, nullptr, nullptr, nullptr, nullptr, dense_thr,
-                                                             cancel_eps, ctr, list,
-                                                             reinterpret_cast<unsigned*>(ctr + 1));
-#undef MIXED_ARGS
+        c3_numeric_kernel<float, false, true><<<grid, 256, 0, h->stream>>>(REG_ARGS, nullptr, nullptr, nullptr, nullptr,
+                                                                           dense_thr, dense_tiles, n_dense);
+#undef REG_ARGS
+    SPG_CUDA(h, cudaGetLastError());
+    int nd_tiles = 0;
+    SPG_TRY(spg_read_i32(h, reinterpret_cast<const int*>(n_dense), &nd_tiles));
+    // 2. the listed tiles' dense pairs on tensor cores, added to their values
+    if (nd_tiles > 0) {
+        const int g2 = grid_cap(h, nd_tiles, 8, 32);
+#define TENSOR_ARGS                                                                                                \
+    nd_tiles, dense_tiles, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,            \
+        B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz, C->tile_nnzC, C->maskC, C->ptrRowC, (float*)C->tile_valC
+        if (cache)
+            c3_tensor_kernel<true><<<g2, 256, 0, h->stream>>>(TENSOR_ARGS, pp->spec_cnt, pp->spec_off, pp->spec_pa,
+                                                               pp->spec_pb, dense_thr, cancel_eps, ctr, list,
+                                                               reinterpret_cast<unsigned*>(ctr + 1), fragA, slotA,
+                                                               fragB, slotB);
+        else
+            c3_tensor_kernel<false><<<g2, 256, 0, h->stream>>>(TENSOR_ARGS, nullptr, nullptr, nullptr, nullptr,
+                                                                dense_thr, cancel_eps, ctr, list,
+                                                                reinterpret_cast<unsigned*>(ctr + 1), fragA, slotA,
+                                                                fragB, slotB);
+#undef TENSOR_ARGS
+    }
+    spg_free_async(h, dense_tiles);
     SPG_CUDA(h, cudaGetLastError());
     int64_t v[2] = {0, 0};
     SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 20, ctr, 16, cudaMemcpyDeviceToHost, h->stream));
@@ -890,5 +963,9 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
     }
     spg_free_async(h, ctr);
     spg_free_async(h, list);
+    spg_free_async(h, slotA);
+    spg_free_async(h, slotB);
+    spg_free_async(h, fragA);
+    spg_free_async(h, fragB);
     return SPG_OK;
 }

@@ -96,7 +96,6 @@ scan_lookback_kernel(const Tin* in, Tout* out, int64_t n, unsigned long long* st
 // coalesced, and the traffic is two reads and one write of the array.
 constexpr int WS_THREADS = 256;
 constexpr int WS_SLICE = 1024;  // items per warp
-constexpr int WS_TILE = WS_SLICE * (WS_THREADS / 32);
 constexpr int64_t WS_MIN_N = 1 << 22;
 
 template <typename Tin>

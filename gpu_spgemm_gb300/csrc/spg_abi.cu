@@ -329,6 +329,15 @@ extern "C" spg_status spg_symbolic(spg_handle_t h, const spg_tiles* A, const spg
     return s;
 }
 
+extern "C" spg_status spg_set_mixed_params(spg_handle_t h, int dense_thr, float cancel_eps) {
+    if (!h) return SPG_ERR_INVALID;
+    if (dense_thr < 1 || dense_thr > 256 || !(cancel_eps >= 0.f) || cancel_eps >= 1.f)
+        return spg_fail(h, SPG_ERR_INVALID, "mixed params: dense_thr in [1, 256], cancel_eps in [0, 1)");
+    h->dense_thr = dense_thr;
+    h->cancel_eps = cancel_eps;
+    return SPG_OK;
+}
+
 extern "C" spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                                   spg_precision prec, spg_ctiles* C) {
     SPG_TRY(validate_pair(h, A, B, C));

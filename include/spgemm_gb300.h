@@ -177,6 +177,12 @@ spg_status spg_tiles_free(spg_handle_t h, spg_tiles* t);
 spg_status spg_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                         spg_ctiles* C);
 
+/* SPG_PREC_MIXED parameters: tile pairs whose A and B tiles both hold >=
+ * dense_thr nonzeros run on the tensor cores (default 32); C tiles with an
+ * entry below cancel_eps times its magnitude sum are recomputed in FP64
+ * (default 2^-20).  No reference counterpart (the reference is FP64 only). */
+spg_status spg_set_mixed_params(spg_handle_t h, int dense_thr, float cancel_eps);
+
 /* Replaces step 3 (step3_numeric_kernel_v2, src/spgemm_raw_kernels_v2.cuh:10-139,
  * launched at src/spgemm_raw_v2.cu:228-238): fills tile_valC and tile_colC. */
 spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
