@@ -1,5 +1,7 @@
 """Device conversions: CSR transpose (the --aat path), tile->CSR export, and the
 Galerkin triple product P^T (A P) chained on the device."""
+import os
+
 import numpy as np
 import pytest
 
@@ -78,3 +80,25 @@ def test_galerkin_matches_oracle(handle, g):
     import scipy.sparse as sp
     G = sp.csr_matrix((gv, gci, grp), shape=R.shape)
     assert abs(G - R).max() <= 1e-5 * abs(R).max()
+
+
+@pytest.mark.skipif(not os.path.exists(api.SIZING_MODEL_PATH), reason="no trained sizing model shipped")
+def test_galerkin_with_learned_sizing_same_structure(handle):
+    """The Galerkin triple product with the trained sizing model attached
+    (learned per-row slots in both products' step 1) equals the exact run."""
+    g = 16
+    a = synth.poisson3d(g)
+    p = synth.smoothed_aggregation(a, synth.aggregation_p0(g))
+    ref, _ = api.galerkin(handle, a, p)
+    ref_h = ref.to_host()
+    model = api.SizingModel.load(handle)
+    model.attach()
+    try:
+        C, _ = api.galerkin(handle, a, p)
+        got = C.to_host()
+    finally:
+        model.detach()
+        model.free()
+    for k in STRUCT_KEYS:
+        np.testing.assert_array_equal(got[k], ref_h[k], err_msg=k)
+    assert rel(got["tile_valC"], ref_h["tile_valC"]) <= 1e-6

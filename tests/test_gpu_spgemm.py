@@ -190,3 +190,23 @@ def test_long_tile_scan_is_exact(handle):
     assert got["tile_nnzC"][0] == 0
     np.testing.assert_array_equal(np.diff(got["tile_nnzC"]), pc)
     assert got["tile_nnzC"][-1] == got["nnzC"]
+
+
+def test_mixed_params_threshold_and_validation(handle):
+    """spg_set_mixed_params: out-of-range arguments are rejected; a lower
+    tensor-core threshold routes more pairs to the tensor cores and the
+    result stays within the FP32 tolerance with exact structure."""
+    from gpu_spgemm_gb300 import _lib as L
+    for bad in ((0, 1e-6), (257, 1e-6), (32, -1.0), (32, 1.0)):
+        with pytest.raises(L.SpgError):
+            handle.set_mixed_params(*bad)
+    a = synth.stencil27_dof3(8)
+    try:
+        handle.set_mixed_params(200)  # above any tile's nonzeros: no tensor-core pairs
+        check_product(handle, a, a, "plain", np.float32, prec="mixed")
+        assert handle.stats()["tensor_pairs"] == 0
+        handle.set_mixed_params(8)
+        check_product(handle, a, a, "plain", np.float32, prec="mixed")
+        assert handle.stats()["tensor_pairs"] > 0
+    finally:
+        handle.set_mixed_params(32, 2.0 ** -20)
