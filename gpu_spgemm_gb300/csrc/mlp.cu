@@ -5,12 +5,13 @@
 // the host and only then fills the tile indices in a second bitmap pass
 // (src/spgemm_raw_v2.cu:119-156).  Here a small MLP reads cheap per-tile-row
 // features of A and B and predicts each tile-row's C tile count and C
-// nonzeros.  The predicted totals pre-size C's arrays, so step 1 runs as ONE
-// fused pass (count, decoupled look-back prefix over tile-rows, fill).  The
-// exact bitmap count inside that pass stays the judge: when the prediction was
-// too small the fused pass has still produced the exact tile_ptrC, and the
-// fill is re-run into exactly sized arrays (overflow re-run).  The structure is
-// never approximated.
+// nonzeros.  Each tile-row then gets a slot of its predicted size (times a
+// margin), and step 1 builds every tile-row's bitmap ONCE: it counts exactly,
+// writes the tile columns into the slot when they fit, and a compaction copies
+// the slots into C's exact arrays (plain.cu, c1_slot_kernel and
+// c1_compact_kernel).  The exact bitmap count stays the judge: a tile-row that
+// outgrew its slot re-runs the exact fill.  The structure is never
+// approximated.
 //
 // Network: 8 -> 32 -> 32 -> 2, ReLU, linear output, MSE on standardised
 // log1p targets.  Trained on the GPU by the kernels below (forward, backward
