@@ -130,7 +130,7 @@ typedef struct {
     float ms_step3;             /* numeric                                     */
     int64_t products;           /* sum over A nonzeros of nnz(B row)           */
     int64_t overflow_reruns;    /* re-runs: pair cache, or tile-rows that outgrew their predicted slot */
-    int64_t work_items;         /* row-wise windows launched                   */
+    int64_t work_items;         /* row-wise work items: (C tile-row, region) pairs */
     int64_t tensor_pairs;       /* tile pairs computed on tensor cores         */
     int64_t fp64_tiles;         /* C tiles recomputed in FP64                  */
     int32_t algo_used;          /* spg_algo the symbolic phase ran             */
