@@ -375,11 +375,11 @@ def measure_e2e(h, api, a, b, args, flops, stream):
     are copied from pinned host memory to the device and tiled, C = A*B is
     computed, and every array of C is copied back to pinned host memory.  C can
     exceed host memory (R-MAT 2^20: ~160 GB), so it streams through fixed
-    pinned staging areas in tile ranges (spg_ctiles_to_host_range).  C's
-    structure is final when spg_symbolic returns, so copy workers (each with
-    its own handle, stream and staging) take tile ranges of it from a shared
-    counter while spg_numeric runs; the values follow when the numeric phase
-    ends, on the same workers."""
+    pinned staging areas in tile ranges (spg_ctiles_to_host_range).  Copy
+    workers (each with its own handle, stream and staging) take tile ranges
+    from a shared counter in three passes: C's tile indices while the mask
+    step (spg_symbolic_masks) runs, the masks, row offsets and nonzero prefix
+    while spg_numeric runs, and the values when the numeric phase ends."""
     import threading
     import ctypes as C
     import torch
@@ -411,9 +411,10 @@ def measure_e2e(h, api, a, b, args, flops, stream):
     workers = [Worker() for _ in range(NW)]
     tstat = {}
 
-    def run_workers(c, want_struct):
-        """Copies C's structure (want_struct) or values in tile ranges taken
-        from a shared counter by every worker; returns the bytes copied."""
+    def run_workers(c, kind):
+        """Copies one part of C ("index": tile row/column indices, "mask":
+        masks, row offsets and nonzero prefix, "value": values and column
+        bytes) in tile ranges taken from a shared counter by every worker."""
         lock = threading.Lock()
         nxt = [0]
         nb = [0]
@@ -434,19 +435,22 @@ def measure_e2e(h, api, a, b, args, flops, stream):
                         step = t1 - t0
                         while True:
                             e = min(t1, t0 + step)
-                            if want_struct:
-                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, g("r"), g("c"), g("m"),
-                                                                  g("p"), g("pr"), None, None, VC, C.byref(nv))
+                            if kind == "index":
+                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, g("r"), g("c"), None,
+                                                                  None, None, None, None, VC, None)
+                            elif kind == "mask":
+                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, g("m"),
+                                                                  g("p"), g("pr"), None, None, VC, None)
                             else:
                                 s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, None, None,
                                                                   None, g("v"), g("cc"), VC, C.byref(nv))
-                            if s_ == L.SPG_ERR_INVALID and not want_struct and step > 1:
+                            if s_ == L.SPG_ERR_INVALID and kind == "value" and step > 1:
                                 step //= 2
                                 continue
                             wk.h.check(s_)
                             break
-                        b_ = (e - t0) * (4 + 4 + 32 + 8 + 16) + 8 if want_struct else \
-                            nv.value * (np.dtype(vd).itemsize + 1)
+                        b_ = {"index": (e - t0) * (4 + 4), "mask": (e - t0) * (32 + 8 + 16) + 8,
+                              "value": nv.value * (np.dtype(vd).itemsize + 1) if kind == "value" else 0}[kind]
                         with lock:
                             nb[0] += b_
                         t0 = e
@@ -464,29 +468,36 @@ def measure_e2e(h, api, a, b, args, flops, stream):
                                            ha[2][1].ctypes.data, code, L.SPG_LAYOUT_ROW, 0, C.byref(ta)))
         h.check(lib.spg_tile_from_csr_host(h.h, b.m, b.n, b.nnz, hb[0][1].ctypes.data, hb[1][1].ctypes.data,
                                            hb[2][1].ctypes.data, code, L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
-        h.check(lib.spg_symbolic(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], C.byref(c)))
+        h.check(lib.spg_symbolic_tiles(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], C.byref(c)))
         tp = np.zeros(c.tilem + 1, np.int32)
         h.check(lib.spg_ctiles_to_host(h.h, C.byref(c), tp.ctypes.data, None, None, None, None, None, None, None))
         t = time.perf_counter()
-        ths, nbs, errs = run_workers(c, True)
+        ths, nbi, errs = run_workers(c, "index")
+        h.check(lib.spg_symbolic_masks(h.h, C.byref(ta), C.byref(tb), C.byref(c)))
+        t_msk = time.perf_counter()
+        for th in ths:
+            th.join()
+        t_idx = time.perf_counter()
+        ths, nbm, errs2 = run_workers(c, "mask")
         h.check(lib.spg_numeric(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], api._PRECS[args.prec],
                                 C.byref(c)))
         t_num = time.perf_counter()
         for th in ths:
             th.join()
         t_struct = time.perf_counter()
-        ths2, nbv, errs2 = run_workers(c, False)
-        for th in ths2:
+        ths, nbv, errs3 = run_workers(c, "value")
+        for th in ths:
             th.join()
         t_val = time.perf_counter()
-        if errs or errs2:
-            raise (errs + errs2)[0]
-        tstat.update(numeric_ms=(t_num - t) * 1e3, structure_copy_ms=(t_struct - t) * 1e3,
+        if errs or errs2 or errs3:
+            raise (errs + errs2 + errs3)[0]
+        tstat.update(mask_step_ms=(t_msk - t) * 1e3, index_copy_ms=(t_idx - t) * 1e3,
+                     numeric_ms=(t_num - t_idx) * 1e3, mask_copy_ms=(t_struct - t_idx) * 1e3,
                      values_copy_ms=(t_val - t_struct) * 1e3)
         lib.spg_ctiles_free(h.h, C.byref(c))
         lib.spg_tiles_free(h.h, C.byref(ta))
         lib.spg_tiles_free(h.h, C.byref(tb))
-        return tp.nbytes + nbs[0] + nbv[0]
+        return tp.nbytes + nbi[0] + nbm[0] + nbv[0]
 
     try:
         one()
@@ -500,9 +511,10 @@ def measure_e2e(h, api, a, b, args, flops, stream):
         dt = (time.perf_counter() - t0) / steps
         return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": dt * 1e3, "steps": steps, "last_step": {k: round(v, 1) for k, v in tstat.items()},
-                "path": "spg_tile_from_csr_host x2 + spg_symbolic + spg_numeric; C to pinned host staging by "
-                        "spg_ctiles_to_host_range on %d copy handles/streams: structure during the numeric "
-                        "phase, values after it (%d tiles per range)" % (NW, CT)}
+                "path": "spg_tile_from_csr_host x2 + spg_symbolic_tiles + spg_symbolic_masks + spg_numeric; C "
+                        "to pinned host staging by spg_ctiles_to_host_range on %d copy handles/streams: tile "
+                        "indices during the mask step, masks during the numeric phase, values after it "
+                        "(%d tiles per range)" % (NW, CT)}
     except Exception as e:  # report instead of dying
         return {"value": None, "unit": "GFLOP/s", "error": str(e)[:200], "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": None}

@@ -94,6 +94,8 @@ SIGNATURES = {
     "spg_mlp_train": (I32, [P, P, P, P, I64, P, I32, I32, C.c_float, P]),
     "spg_set_sizing_model": (I32, [P, P, C.c_float]),
     "spg_set_mixed_params": (I32, [P, C.c_int, C.c_float]),
+    "spg_symbolic_tiles": (I32, [P, P, P, C.c_int, P]),
+    "spg_symbolic_masks": (I32, [P, P, P, P]),
     "spg_galerkin": (I32, [P, I32, I32, I64, P, P, P, I64, P, P, P, I32, I32, I32, C.POINTER(SpgCTiles),
                            C.POINTER(I64)]),
 }

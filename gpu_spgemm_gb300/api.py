@@ -211,6 +211,19 @@ def symbolic(handle: Handle, A: TileMatrix, B: TileMatrix, algo: str = "auto") -
     return CTileMatrix(handle, c)
 
 
+def symbolic_tiles(handle: Handle, A: TileMatrix, B: TileMatrix, algo: str = "auto") -> CTileMatrix:
+    """Step 1 alone (src/spgemm_raw_v2.cu:111-158): C's tile structure."""
+    c = L.SpgCTiles()
+    handle.check(handle.lib.spg_symbolic_tiles(handle.h, C.byref(A.t), C.byref(B.t), _ALGOS[algo], C.byref(c)))
+    return CTileMatrix(handle, c)
+
+
+def symbolic_masks(handle: Handle, A: TileMatrix, B: TileMatrix, Cm: CTileMatrix) -> CTileMatrix:
+    """Step 2 on a C from symbolic_tiles (src/spgemm_raw_v2.cu:160-221)."""
+    handle.check(handle.lib.spg_symbolic_masks(handle.h, C.byref(A.t), C.byref(B.t), C.byref(Cm.c)))
+    return Cm
+
+
 def numeric(handle: Handle, A: TileMatrix, B: TileMatrix, Cm: CTileMatrix, algo: str = "auto",
             prec: str = "f32") -> CTileMatrix:
     """Step 3 (src/spgemm_raw_v2.cu:223-243)."""

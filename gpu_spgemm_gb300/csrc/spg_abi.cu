@@ -243,8 +243,9 @@ extern "C" spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C) {
     return SPG_OK;
 }
 
-static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
-                                spg_ctiles* C) {
+// Step 1: C's tile structure (tile_ptrC, tile_rowidxC, tile_colidxC).
+static spg_status tiles_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                             spg_ctiles* C) {
     *C = spg_ctiles{};
     C->m = A->m; C->n = B->n; C->tilem = A->tilem; C->tilen = B->tilen; C->dtype = A->dtype;
     CPriv* cp = new (std::nothrow) CPriv();
@@ -268,6 +269,17 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
     } else {
         SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
     }
+    SPG_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+    SPG_CUDA(h, cudaEventSynchronize(h->ev[1]));
+    h->stats.ms_step1 = elapsed(h, 0, 1);
+    return spg_check_flags(h, "symbolic step 1");
+}
+
+// Step 2 on C's tile structure from tiles_impl: masks, row offsets, tile
+// nonzero prefix, value arrays.
+static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C) {
+    CPriv* cp = static_cast<CPriv*>(C->priv);
+    const spg_algo algo = cp->algo;
     SPG_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
     const int64_t nt = C->numtileC;
     // ---- step 2: bitmask symbolic
@@ -315,9 +327,14 @@ static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_ti
     }
     SPG_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
     SPG_CUDA(h, cudaEventSynchronize(h->ev[2]));
-    h->stats.ms_step1 = elapsed(h, 0, 1);
     h->stats.ms_step2 = elapsed(h, 1, 2);
     return spg_check_flags(h, "symbolic");
+}
+
+static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                                spg_ctiles* C) {
+    SPG_TRY(tiles_impl(h, A, B, algo, C));
+    return masks_impl(h, A, B, C);
 }
 
 extern "C" spg_status spg_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
@@ -338,10 +355,30 @@ extern "C" spg_status spg_set_mixed_params(spg_handle_t h, int dense_thr, float 
     return SPG_OK;
 }
 
+extern "C" spg_status spg_symbolic_tiles(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                                         spg_ctiles* C) {
+    SPG_TRY(validate_pair(h, A, B, C));
+    h->stats = spg_stats{};
+    spg_status s = tiles_impl(h, A, B, algo, C);
+    if (s != SPG_OK) { std::string e = h->err; spg_ctiles_free(h, C); h->err = e; }
+    return s;
+}
+
+extern "C" spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C) {
+    SPG_TRY(validate_pair(h, A, B, C));
+    if (!C->priv || (!C->tile_colidxC && C->numtileC > 0) || C->maskC)
+        return spg_fail(h, SPG_ERR_INVALID, "symbolic masks: C must come from spg_symbolic_tiles");
+    spg_status s = masks_impl(h, A, B, C);
+    if (s != SPG_OK) { std::string e = h->err; spg_ctiles_free(h, C); h->err = e; }
+    return s;
+}
+
 extern "C" spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                                   spg_precision prec, spg_ctiles* C) {
     SPG_TRY(validate_pair(h, A, B, C));
     if (!C->priv) return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic structure");
+    if (C->numtileC > 0 && (!C->maskC || !C->tile_nnzC || !C->tile_valC))
+        return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
     CPriv* cp = static_cast<CPriv*>(C->priv);
     if (algo == SPG_ALGO_AUTO) algo = cp->algo;
     if (algo == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) algo = SPG_ALGO_PLAIN;
@@ -408,7 +445,9 @@ extern "C" spg_status spg_ctiles_to_host_range(spg_handle_t h, const spg_ctiles*
     if (!h || !C) return SPG_ERR_INVALID;
     if (tb < 0 || te < tb || te > C->numtileC) return spg_fail(h, SPG_ERR_INVALID, "range: bad tile range");
     int64_t v0 = 0, v1 = 0;
-    if (C->numtileC > 0) {
+    const bool need_nnz = tile_valC || tile_colC || tile_nnzC || n_values;
+    if (need_nnz && C->numtileC > 0) {
+        if (!C->tile_nnzC) return spg_fail(h, SPG_ERR_INVALID, "range: C has no symbolic masks yet");
         SPG_TRY(spg_read_i64(h, C->tile_nnzC + tb, &v0));
         SPG_TRY(spg_read_i64(h, C->tile_nnzC + te, &v1));
     }

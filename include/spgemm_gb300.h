@@ -183,6 +183,16 @@ spg_status spg_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, 
  * (default 2^-20).  No reference counterpart (the reference is FP64 only). */
 spg_status spg_set_mixed_params(spg_handle_t h, int dense_thr, float cancel_eps);
 
+/* spg_symbolic in its two steps.  spg_symbolic_tiles is step 1: C's tile
+ * structure (tile_ptrC, tile_rowidxC, tile_colidxC, numtileC;
+ * src/spgemm_raw_v2.cu:111-158).  spg_symbolic_masks on that C is step 2:
+ * maskC, ptrRowC, tile_nnzC, nnzC and the value arrays (:160-221).  Called
+ * separately, a caller can start copying C's tile indices while step 2 runs,
+ * e.g. with spg_ctiles_to_host_range on another handle. */
+spg_status spg_symbolic_tiles(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                              spg_ctiles* C);
+spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C);
+
 /* Replaces step 3 (step3_numeric_kernel_v2, src/spgemm_raw_kernels_v2.cuh:10-139,
  * launched at src/spgemm_raw_v2.cu:228-238): fills tile_valC and tile_colC. */
 spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,

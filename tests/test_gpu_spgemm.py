@@ -210,3 +210,40 @@ def test_mixed_params_threshold_and_validation(handle):
         assert handle.stats()["tensor_pairs"] > 0
     finally:
         handle.set_mixed_params(32, 2.0 ** -20)
+
+
+@pytest.mark.parametrize("algo", ["plain", "rowwise"])
+def test_split_symbolic_matches_one_call(handle, algo):
+    """spg_symbolic_tiles then spg_symbolic_masks give the product spg_symbolic
+    gives.  C's tile indices copy out between the two calls; the prefix and
+    the values cannot, spg_numeric refuses a C without masks, and a second
+    spg_symbolic_masks on the same C is refused without freeing it."""
+    import ctypes as C
+    from gpu_spgemm_gb300 import _lib as L
+    lib = handle.lib
+    a = synth.rmat(12, 16).astype(np.float32)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    S = oracle.spgemm_tiles(a, a)
+    Cm = api.symbolic_tiles(handle, A, B, algo=algo)
+    nt = Cm.numtileC
+    assert nt == S["numtileC"]
+    P = lambda x: x.ctypes.data_as(C.c_void_p)
+    r, c = np.zeros(nt, np.int32), np.zeros(nt, np.int32)
+    handle.check(lib.spg_ctiles_to_host_range(handle.h, C.byref(Cm.c), 0, nt, P(r), P(c), None, None, None,
+                                              None, None, 0, None))
+    np.testing.assert_array_equal(r, S["tile_rowidxC"])
+    np.testing.assert_array_equal(c, S["tile_colidxC"])
+    nv = C.c_int64()
+    assert lib.spg_ctiles_to_host_range(handle.h, C.byref(Cm.c), 0, nt, None, None, None, None, None, None, None,
+                                        0, C.byref(nv)) == L.SPG_ERR_INVALID
+    assert lib.spg_numeric(handle.h, C.byref(A.t), C.byref(B.t), api._ALGOS[algo], api._PRECS["f32"],
+                           C.byref(Cm.c)) == L.SPG_ERR_INVALID
+    api.symbolic_masks(handle, A, B, Cm)
+    assert lib.spg_symbolic_masks(handle.h, C.byref(A.t), C.byref(B.t), C.byref(Cm.c)) == L.SPG_ERR_INVALID
+    api.numeric(handle, A, B, Cm, algo=algo)
+    got = Cm.to_host()
+    assert got["nnzC"] == S["nnzC"]
+    for k in STRUCT_KEYS:
+        np.testing.assert_array_equal(got[k], S[k].astype(got[k].dtype), err_msg=k)
+    assert rel_frob(got["tile_valC"], S["tile_valC"]) <= TOL[np.float32]
