@@ -373,13 +373,19 @@ def gpu_launches(algo):
 def measure_e2e(h, api, a, b, args, flops, stream):
     """End to end through the C ABI with host buffers, per step: the CSR inputs
     are copied from pinned host memory to the device and tiled, C = A*B is
-    computed, and every array of C is copied back to pinned host memory.  C can
-    exceed host memory (R-MAT 2^20: ~160 GB), so it streams through fixed
-    pinned staging areas in tile ranges (spg_ctiles_to_host_range).  Copy
-    workers (each with its own handle, stream and staging) take tile ranges
-    from a shared counter in three passes: C's tile indices while the mask
-    step (spg_symbolic_masks) runs, the masks, row offsets and nonzero prefix
-    while spg_numeric runs, and the values when the numeric phase ends."""
+    computed, and C's result is copied back to pinned host memory: the arrays
+    the reference reads back for its result (src/spgemm_raw_v2.cu:257-266):
+    tile_ptrC, tile_rowidxC, tile_colidxC, the nonzero prefix tile_nnzC, the
+    column bytes tile_colC and the values tile_valC.  (maskC and ptrRowC are
+    intermediates that tile_colC restates; they stay on the device.)  C can
+    exceed host memory (R-MAT 2^20: ~77 GB of result), so it streams through
+    fixed pinned staging in tile ranges (spg_ctiles_to_host_range) on copy
+    workers, each with its own handle, stream and staging, fed from one FIFO
+    as the arrays become final: the tile indices when spg_symbolic_tiles
+    returns (copied while spg_symbolic_masks runs), the prefix when the masks
+    are done, and each band of tile-rows' values as spg_numeric_bands reports
+    the band complete (copied while the numeric launch goes on)."""
+    import queue
     import threading
     import ctypes as C
     import torch
@@ -393,10 +399,12 @@ def measure_e2e(h, api, a, b, args, flops, stream):
     hb = [pin(b.row_ptr), pin(b.col_idx), pin(b.val)]
     code = L.SPG_F64 if a.val.dtype == np.float64 else L.SPG_F32
     vd = np.float64 if code == L.SPG_F64 else np.float32
+    vsz = np.dtype(vd).itemsize
     h2d = sum(x[1].nbytes for x in ha + hb)
     CT = 1 << 23            # C tiles per staged range
     VC = 1 << 27            # values per staged range (ranges halve when a range holds more)
     NW = max(1, args.e2e_copy_workers)
+    NB = max(1, args.e2e_bands)
     lib = h.lib
 
     class Worker:
@@ -404,63 +412,41 @@ def measure_e2e(h, api, a, b, args, flops, stream):
             self.stream = torch.cuda.Stream()
             self.h = api.Handle(torch.cuda.current_device(), self.stream)
             self.st = dict(r=pin(np.zeros(CT, np.int32)), c=pin(np.zeros(CT, np.int32)),
-                           m=pin(np.zeros(CT * TS, np.uint16)), p=pin(np.zeros(CT + 1, np.int64)),
-                           pr=pin(np.zeros(CT * TS, np.uint8)), v=pin(np.zeros(VC, vd)),
+                           p=pin(np.zeros(CT + 1, np.int64)), v=pin(np.zeros(VC, vd)),
                            cc=pin(np.zeros(VC, np.uint8)))
 
     workers = [Worker() for _ in range(NW)]
     tstat = {}
 
-    def run_workers(c, kind):
-        """Copies one part of C ("index": tile row/column indices, "mask":
-        masks, row offsets and nonzero prefix, "value": values and column
-        bytes) in tile ranges taken from a shared counter by every worker."""
-        lock = threading.Lock()
-        nxt = [0]
-        nb = [0]
-        errs = []
-
-        def work(wk):
-            nv = C.c_int64()
-            g = lambda k: wk.st[k][1].ctypes.data
-            try:
-                while True:
-                    with lock:
-                        t0 = nxt[0]
-                        if t0 >= c.numtileC:
-                            return
-                        t1 = min(c.numtileC, t0 + CT)
-                        nxt[0] = t1
-                    while t0 < t1:  # a value range holding more than VC values is cut in halves
-                        step = t1 - t0
-                        while True:
-                            e = min(t1, t0 + step)
-                            if kind == "index":
-                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, g("r"), g("c"), None,
-                                                                  None, None, None, None, VC, None)
-                            elif kind == "mask":
-                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, g("m"),
-                                                                  g("p"), g("pr"), None, None, VC, None)
-                            else:
-                                s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, None, None,
-                                                                  None, g("v"), g("cc"), VC, C.byref(nv))
-                            if s_ == L.SPG_ERR_INVALID and kind == "value" and step > 1:
-                                step //= 2
-                                continue
-                            wk.h.check(s_)
-                            break
-                        b_ = {"index": (e - t0) * (4 + 4), "mask": (e - t0) * (32 + 8 + 16) + 8,
-                              "value": nv.value * (np.dtype(vd).itemsize + 1) if kind == "value" else 0}[kind]
-                        with lock:
-                            nb[0] += b_
-                        t0 = e
-            except Exception as ex:
-                errs.append(ex)
-
-        ths = [threading.Thread(target=work, args=(wk,)) for wk in workers]
-        for t in ths:
-            t.start()
-        return ths, nb, errs
+    def copy_range(wk, c, kind, t0, t1):
+        """One staged copy of C tiles [t0, t1): "index" (tile row and column
+        indices), "prefix" (tile_nnzC) or "value" (values and column bytes,
+        split in halves while a range holds more than VC values)."""
+        nv = C.c_int64()
+        g = lambda k: wk.st[k][1].ctypes.data
+        nb = 0
+        while t0 < t1:
+            step = t1 - t0
+            while True:
+                e = min(t1, t0 + step)
+                if kind == "index":
+                    s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, g("r"), g("c"), None, None, None,
+                                                      None, None, VC, None)
+                elif kind == "prefix":
+                    s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, None, g("p"), None,
+                                                      None, None, VC, None)
+                else:
+                    s_ = lib.spg_ctiles_to_host_range(wk.h.h, C.byref(c), t0, e, None, None, None, None, None,
+                                                      g("v"), g("cc"), VC, C.byref(nv))
+                if s_ == L.SPG_ERR_INVALID and kind == "value" and step > 1:
+                    step //= 2
+                    continue
+                wk.h.check(s_)
+                break
+            nb += {"index": (e - t0) * 8, "prefix": (e - t0 + 1) * 8}.get(kind, 0) + \
+                (nv.value * (vsz + 1) if kind == "value" else 0)
+            t0 = e
+        return nb
 
     def one():
         ta, tb, c = L.SpgTiles(), L.SpgTiles(), L.SpgCTiles()
@@ -471,33 +457,79 @@ def measure_e2e(h, api, a, b, args, flops, stream):
         h.check(lib.spg_symbolic_tiles(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], C.byref(c)))
         tp = np.zeros(c.tilem + 1, np.int32)
         h.check(lib.spg_ctiles_to_host(h.h, C.byref(c), tp.ctypes.data, None, None, None, None, None, None, None))
+        q = queue.Queue()
+        nbytes = [tp.nbytes]
+        errs = []
+        lock = threading.Lock()
+        done_at = {}
+
+        def work(wk):
+            while True:
+                task = q.get()
+                if task is None:
+                    return
+                kind, t0, t1 = task
+                try:
+                    if not errs:
+                        ts = time.perf_counter()
+                        nb = copy_range(wk, c, kind, t0, t1)
+                        te = time.perf_counter()
+                        with lock:
+                            nbytes[0] += nb
+                            done_at.setdefault(kind, []).append((ts, te, nb))
+                except Exception as ex:  # reported after the join
+                    errs.append(ex)
+
+        def push(kind, t0, t1):
+            for x in range(t0, t1, CT):
+                q.put((kind, x, min(t1, x + CT)))
+
+        ths = [threading.Thread(target=work, args=(wk,)) for wk in workers]
+        for th in ths:
+            th.start()
         t = time.perf_counter()
-        ths, nbi, errs = run_workers(c, "index")
-        h.check(lib.spg_symbolic_masks(h.h, C.byref(ta), C.byref(tb), C.byref(c)))
-        t_msk = time.perf_counter()
-        for th in ths:
-            th.join()
-        t_idx = time.perf_counter()
-        ths, nbm, errs2 = run_workers(c, "mask")
-        h.check(lib.spg_numeric(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], api._PRECS[args.prec],
-                                C.byref(c)))
-        t_num = time.perf_counter()
-        for th in ths:
-            th.join()
-        t_struct = time.perf_counter()
-        ths, nbv, errs3 = run_workers(c, "value")
-        for th in ths:
-            th.join()
-        t_val = time.perf_counter()
-        if errs or errs2 or errs3:
-            raise (errs + errs2 + errs3)[0]
-        tstat.update(mask_step_ms=(t_msk - t) * 1e3, index_copy_ms=(t_idx - t) * 1e3,
-                     numeric_ms=(t_num - t_idx) * 1e3, mask_copy_ms=(t_struct - t_idx) * 1e3,
-                     values_copy_ms=(t_val - t_struct) * 1e3)
+        try:
+            push("index", 0, c.numtileC)
+            h.check(lib.spg_symbolic_masks(h.h, C.byref(ta), C.byref(tb), C.byref(c)))
+            t_msk = time.perf_counter()
+            push("prefix", 0, c.numtileC)
+            # tile-row bands of about equal tile counts
+            cuts = np.searchsorted(tp, np.linspace(0, c.numtileC, NB + 1)[1:-1], side="left")
+            bounds = [0] + sorted(set(int(x) for x in cuts if 0 < x < c.tilem)) + [c.tilem]
+            rows = np.asarray(bounds, np.int32)
+            band_at = []
+
+            def on_band(_u, k, r0, r1):
+                band_at.append((k, time.perf_counter()))
+                push("value", int(tp[r0]), int(tp[r1]))
+
+            fn = L.BAND_FN(on_band)
+            order = L.SPG_BANDS_LAST_TO_FIRST if args.e2e_band_order == "last" else L.SPG_BANDS_FIRST_TO_LAST
+            h.check(lib.spg_numeric_bands(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo],
+                                          api._PRECS[args.prec], C.byref(c), len(bounds) - 1,
+                                          rows.ctypes.data, order, fn, None))
+            t_num = time.perf_counter()
+        finally:
+            for _ in ths:
+                q.put(None)
+            for th in ths:
+                th.join()
+        t_end = time.perf_counter()
+        if errs:
+            raise errs[0]
+        ms = lambda x: round((x - t_msk) * 1e3, 1)
+        # per worker: bytes over the time its copy calls took (workers copy side by side)
+        gbs = lambda v: round(sum(b_ for _, _, b_ in v) / max(1e-9, sum(e_ - s_ for s_, e_, _ in v)) / 1e9, 1)
+        tstat.update(mask_step_ms=(t_msk - t) * 1e3, numeric_bands_ms=(t_num - t_msk) * 1e3,
+                     copy_tail_ms=(t_end - t_num) * 1e3, bands=len(bounds) - 1,
+                     band_done_ms=[ms(x) for _, x in sorted(band_at)],
+                     copy_window_ms={k: [ms(min(s_ for s_, _, _ in v)), ms(max(e_ for _, e_, _ in v))]
+                                     for k, v in done_at.items()},
+                     copy_gbs_per_worker={k: gbs(v) for k, v in done_at.items()})
         lib.spg_ctiles_free(h.h, C.byref(c))
         lib.spg_tiles_free(h.h, C.byref(ta))
         lib.spg_tiles_free(h.h, C.byref(tb))
-        return tp.nbytes + nbi[0] + nbm[0] + nbv[0]
+        return nbytes[0]
 
     try:
         one()
@@ -510,11 +542,13 @@ def measure_e2e(h, api, a, b, args, flops, stream):
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / steps
         return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": dt * 1e3, "steps": steps, "last_step": {k: round(v, 1) for k, v in tstat.items()},
-                "path": "spg_tile_from_csr_host x2 + spg_symbolic_tiles + spg_symbolic_masks + spg_numeric; C "
-                        "to pinned host staging by spg_ctiles_to_host_range on %d copy handles/streams: tile "
-                        "indices during the mask step, masks during the numeric phase, values after it "
-                        "(%d tiles per range)" % (NW, CT)}
+                "ms_per_step": dt * 1e3, "steps": steps,
+                "last_step": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in tstat.items()},
+                "path": "spg_tile_from_csr_host x2 + spg_symbolic_tiles + spg_symbolic_masks + spg_numeric_bands "
+                        "(%d tile-row bands, %s band first); C's result (tile_ptrC, tile_rowidxC, tile_colidxC, tile_nnzC, "
+                        "tile_colC, tile_valC, as the reference reads it back) to pinned host staging by "
+                        "spg_ctiles_to_host_range on %d copy handles/streams as each part becomes final "
+                        "(%d tiles per range)" % (NB, args.e2e_band_order, NW, CT)}
     except Exception as e:  # report instead of dying
         return {"value": None, "unit": "GFLOP/s", "error": str(e)[:200], "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": None}
@@ -610,6 +644,10 @@ def main():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--e2e-bands", type=int, default=8,
+                   help="tile-row bands of the e2e numeric phase (a band's values copy once it is complete)")
+    p.add_argument("--e2e-band-order", choices=["last", "first"], default="last",
+                   help="e2e bands worked on from the last (light rows first, hub rows last) or the first")
     p.add_argument("--e2e-copy-workers", type=int, default=2,
                    help="copy handles/streams/host threads streaming C back in the e2e measurement")
     p.add_argument("--cpu-s", type=float, default=12.0)

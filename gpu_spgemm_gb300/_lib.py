@@ -20,6 +20,7 @@ SPG_LAYOUT_ROW, SPG_LAYOUT_B_CSC = 0, 1
 SPG_TILE_WITH_TILE_CSC = 1
 SPG_ALGO_AUTO, SPG_ALGO_PLAIN, SPG_ALGO_ROWWISE = 0, 1, 2
 SPG_PREC_F32, SPG_PREC_MIXED, SPG_PREC_F64 = 0, 1, 2
+SPG_BANDS_FIRST_TO_LAST, SPG_BANDS_LAST_TO_FIRST = 0, 1
 
 P = C.c_void_p
 I32 = C.c_int
@@ -47,6 +48,9 @@ class SpgStats(C.Structure):
                 ("products", I64), ("overflow_reruns", I64), ("work_items", I64), ("tensor_pairs", I64),
                 ("fp64_tiles", I64), ("algo_used", I32), ("reserved", I32), ("predicted_tiles", I64)]
 
+
+# spg_band_fn: (user, band, row_begin, row_end)
+BAND_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
 
 # name -> (restype, argtypes); every symbol the header declares
 SIGNATURES = {
@@ -96,6 +100,8 @@ SIGNATURES = {
     "spg_set_mixed_params": (I32, [P, C.c_int, C.c_float]),
     "spg_symbolic_tiles": (I32, [P, P, P, C.c_int, P]),
     "spg_symbolic_masks": (I32, [P, P, P, P]),
+    "spg_numeric_rows": (I32, [P, P, P, I32, I32, P, I32, I32]),
+    "spg_numeric_bands": (I32, [P, P, P, I32, I32, P, I32, P, I32, BAND_FN, P]),
     "spg_galerkin": (I32, [P, I32, I32, I64, P, P, P, I64, P, P, P, I32, I32, I32, C.POINTER(SpgCTiles),
                            C.POINTER(I64)]),
 }

@@ -232,6 +232,39 @@ def numeric(handle: Handle, A: TileMatrix, B: TileMatrix, Cm: CTileMatrix, algo:
     return Cm
 
 
+def numeric_rows(handle: Handle, A: TileMatrix, B: TileMatrix, Cm: CTileMatrix, row_begin: int, row_end: int,
+                 algo: str = "auto", prec: str = "f32") -> CTileMatrix:
+    """Step 3 on C tile-rows [row_begin, row_end) (src/spgemm_raw_v2.cu:223-243)."""
+    handle.check(handle.lib.spg_numeric_rows(handle.h, C.byref(A.t), C.byref(B.t), _ALGOS[algo], _PRECS[prec],
+                                             C.byref(Cm.c), int(row_begin), int(row_end)))
+    return Cm
+
+
+def numeric_bands(handle: Handle, A: TileMatrix, B: TileMatrix, Cm: CTileMatrix, band_rows, on_band,
+                  algo: str = "auto", prec: str = "f32", last_first: bool = False) -> CTileMatrix:
+    """Step 3 (src/spgemm_raw_v2.cu:223-243) reporting bands of C tile-rows:
+    on_band(k, row_begin, row_end) runs as soon as band k's values are final
+    (band k = tile-rows [band_rows[k], band_rows[k+1])); last_first works on
+    the last band first."""
+    rows = np.ascontiguousarray(np.asarray(band_rows, dtype=np.int32))
+    errs = []
+
+    def cb(_user, k, r0, r1):
+        try:
+            on_band(k, r0, r1)
+        except Exception as e:  # raised again after the call
+            errs.append(e)
+
+    fn = L.BAND_FN(cb)
+    handle.check(handle.lib.spg_numeric_bands(handle.h, C.byref(A.t), C.byref(B.t), _ALGOS[algo], _PRECS[prec],
+                                              C.byref(Cm.c), len(rows) - 1, _ptr(rows),
+                                              L.SPG_BANDS_LAST_TO_FIRST if last_first else L.SPG_BANDS_FIRST_TO_LAST,
+                                              fn, None))
+    if errs:
+        raise errs[0]
+    return Cm
+
+
 def spgemm(handle: Handle, A: TileMatrix, B: TileMatrix, algo: str = "auto", prec: str = "f32") -> CTileMatrix:
     """Steps 1-3 in one call."""
     c = L.SpgCTiles()

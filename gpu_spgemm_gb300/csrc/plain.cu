@@ -837,39 +837,64 @@ spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     return SPG_OK;
 }
 
+// The per-C-tile arrays seen from tile t0 on: the kernels index them by the
+// tile's position in [t0, t1) and reach values and column bytes through the
+// absolute nonzero prefix, so a tile range needs no other change.
+struct CTileView {
+    const int* rowidx;
+    const int* colidx;
+    const int64_t* nnz;
+    const uint16_t* mask;
+    const uint8_t* ptr16;
+    const int* spec_cnt;
+    const int* spec_off;
+};
+
+static CTileView ctile_view(const spg_ctiles* C, const PlainPriv* pp, int64_t t0) {
+    const bool cache = pp && pp->spec_cap > 0;
+    return CTileView{C->tile_rowidxC + t0, C->tile_colidxC + t0, C->tile_nnzC + t0, C->maskC + t0 * TS,
+                     C->ptrRowC + t0 * TS, cache ? pp->spec_cnt + t0 : nullptr,
+                     cache ? pp->spec_off + t0 : nullptr};
+}
+
 template <typename V>
 static spg_status plain_step3_t(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                                PlainPriv* pp) {
-    const int64_t nt = C->numtileC;
-    if (nt == 0 || C->nnzC == 0) return SPG_OK;
+                                PlainPriv* pp, int64_t t0, int64_t t1) {
+    const int64_t nt = t1 - t0;
+    if (nt <= 0 || C->nnzC == 0) return SPG_OK;
+    const CTileView cv = ctile_view(C, pp, t0);
     const int grid = grid_cap(h, nt, 8, 32);
     if (pp && pp->spec_cap > 0)
         c3_numeric_kernel<V, true><<<grid, 256, 0, h->stream>>>(
-            nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            nt, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
             (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
-            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,
-            (V*)C->tile_valC, C->tile_colC, pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb);
+            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,
+            (V*)C->tile_valC, C->tile_colC, cv.spec_cnt, cv.spec_off, pp->spec_pa, pp->spec_pb);
     else
         c3_numeric_kernel<V, false><<<grid, 256, 0, h->stream>>>(
-            nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            nt, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
             (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
-            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,
+            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,
             (V*)C->tile_valC, C->tile_colC, nullptr, nullptr, nullptr, nullptr);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }
 
-spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp) {
-    if (A->dtype == SPG_F64) return plain_step3_t<double>(h, A, B, C, pp);
-    return plain_step3_t<float>(h, A, B, C, pp);
+spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
+                       int64_t t0, int64_t t1) {
+    if (t1 < 0) t1 = C->numtileC;
+    if (A->dtype == SPG_F64) return plain_step3_t<double>(h, A, B, C, pp, t0, t1);
+    return plain_step3_t<float>(h, A, B, C, pp, t0, t1);
 }
 
 // Mixed-precision numeric (FP32 data): dense tile pairs on tensor cores, the
 // rest on FP32 registers, cancellation-flagged C tiles recomputed in FP64.
 spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
-                             int dense_thr, float cancel_eps) {
-    const int64_t nt = C->numtileC;
-    if (nt == 0 || C->nnzC == 0) return SPG_OK;
+                             int dense_thr, float cancel_eps, int64_t t0, int64_t t1) {
+    if (t1 < 0) t1 = C->numtileC;
+    const int64_t nt = t1 - t0;
+    if (nt <= 0 || C->nnzC == 0) return SPG_OK;
+    const CTileView cv = ctile_view(C, pp, t0);
     if (A->dtype != SPG_F32) return spg_fail(h, SPG_ERR_INVALID, "mixed precision needs FP32 data");
     unsigned long long* ctr = nullptr;
     int* list = nullptr;
@@ -911,13 +936,13 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
     unsigned* n_dense = reinterpret_cast<unsigned*>(ctr) + 3;  // high word of ctr[1]
     SPG_TRY(spg_alloc_t(h, &dense_tiles, (size_t)nt + 1));
 #define REG_ARGS                                                                                                    \
-    nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const float*)A->tile_csr_Val, \
+    nt, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const float*)A->tile_csr_Val,          \
         A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz,                        \
-        (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC, C->ptrRowC,                \
+        (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,                        \
         (float*)C->tile_valC, C->tile_colC
     if (cache)
         c3_numeric_kernel<float, true, true><<<grid, 256, 0, h->stream>>>(
-            REG_ARGS, pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb, dense_thr, dense_tiles, n_dense);
+            REG_ARGS, cv.spec_cnt, cv.spec_off, pp->spec_pa, pp->spec_pb, dense_thr, dense_tiles, n_dense);
     else
         c3_numeric_kernel<float, false, true><<<grid, 256, 0, h->stream>>>(REG_ARGS, nullptr, nullptr, nullptr, nullptr,
                                                                            dense_thr, dense_tiles, n_dense);
@@ -929,10 +954,10 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
     if (nd_tiles > 0) {
         const int g2 = grid_cap(h, nd_tiles, 8, 32);
 #define TENSOR_ARGS                                                                                                \
-    nd_tiles, dense_tiles, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,            \
-        B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz, C->tile_nnzC, C->maskC, C->ptrRowC, (float*)C->tile_valC
+    nd_tiles, dense_tiles, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz,                        \
+        B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz, cv.nnz, cv.mask, cv.ptr16, (float*)C->tile_valC
         if (cache)
-            c3_tensor_kernel<true><<<g2, 256, 0, h->stream>>>(TENSOR_ARGS, pp->spec_cnt, pp->spec_off, pp->spec_pa,
+            c3_tensor_kernel<true><<<g2, 256, 0, h->stream>>>(TENSOR_ARGS, cv.spec_cnt, cv.spec_off, pp->spec_pa,
                                                                pp->spec_pb, dense_thr, cancel_eps, ctr, list,
                                                                reinterpret_cast<unsigned*>(ctr + 1), fragA, slotA,
                                                                fragB, slotB);
@@ -955,10 +980,10 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
     if (v[1] > 0) {
         const int g2 = grid_cap(h, v[1], 8, 32);
         c3_fp64_list_kernel<<<g2, 256, 0, h->stream>>>(
-            (int)v[1], list, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            (int)v[1], list, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
             (const float*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
-            B->tile_nnz, (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, C->tile_nnzC, C->maskC,
-            C->ptrRowC, (float*)C->tile_valC);
+            B->tile_nnz, (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask,
+            cv.ptr16, (float*)C->tile_valC);
         SPG_CUDA(h, cudaGetLastError());
     }
     spg_free_async(h, ctr);

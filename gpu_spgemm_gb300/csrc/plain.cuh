@@ -21,10 +21,11 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
 spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz);
 spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                        PlainPriv* pp, int* tile_cnt);
+// Step 3 on C tiles [t0, t1) (t1 < 0: every tile).
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                       PlainPriv* pp);
+                       PlainPriv* pp, int64_t t0 = 0, int64_t t1 = -1);
 spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
-                             int dense_thr, float cancel_eps);
+                             int dense_thr, float cancel_eps, int64_t t0 = 0, int64_t t1 = -1);
 
 spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int* d_rp, const int* d_ci,
                            const void* d_val, spg_dtype dtype, spg_layout layout, int flags, spg_tiles* out);

@@ -82,14 +82,16 @@ __global__ void rw_plan_kernel(int tilem, int m, const int* __restrict__ tile_pt
 }
 
 // Plan, pass 2: work items per tile-row.  A tile-row is cut into regions of
-// at most RT C tiles and at most ~PW products, PW = total / (SMs * 16) (at
+// at most RT C tiles and at most ~PW products, PW = total / (SMs * 64) (at
 // least 2^16): hub tile-rows of a power-law matrix become many balanced
-// items instead of one long one.
+// items instead of one long one, so no item holds up the end of a launch or
+// of a band of tile-rows.  (Each item re-seeks its A nonzeros' cursors:
+// R-MAT 2^20 gets 140,774 items instead of 139,942 at SMs * 16.)
 __global__ void rw_plan2_kernel(int tilem, int num_sms, const int* __restrict__ tile_ptrC,
                                 const int64_t* __restrict__ prod, const unsigned long long* __restrict__ total,
                                 int64_t* __restrict__ nitems) {
     const unsigned long long tot = *total;
-    unsigned long long pw = tot / ((unsigned long long)num_sms * 16ull);
+    unsigned long long pw = tot / ((unsigned long long)num_sms * 64ull);
     if (pw < (1ull << 16)) pw = 1ull << 16;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
         const int64_t ntc = tile_ptrC[i + 1] - tile_ptrC[i];
@@ -107,18 +109,37 @@ __global__ void rw_plan2_kernel(int tilem, int num_sms, const int* __restrict__ 
 
 // Shared state of one work item.
 struct ItemInfo {
+    long long id;
     int i, rs, re, e0, na, q;
 };
 
-// Takes the next work item; returns false when none is left.  All threads call.
+// Takes the next work item of [item_lo, item_hi); returns false when none is
+// left.  All threads call.  With rev_bands > 0 (and item_lo == 0) tickets run
+// through the bands of band_end from the last band to the first, each band's
+// items in order: ticket x lies in band b when band_start[b] < item_hi - x <=
+// band_end[b].
 __device__ bool next_item(unsigned long long* ticket, const int64_t* __restrict__ item_prefix, int tilem,
-                          int64_t nitems, const int* __restrict__ tile_ptrC, const int* __restrict__ a_rp, int m,
-                          ItemInfo* s_it, int* s_rows) {
+                          int64_t item_lo, int64_t item_hi, const int* __restrict__ tile_ptrC,
+                          const int* __restrict__ a_rp, int m, ItemInfo* s_it, int* s_rows, int rev_bands = 0,
+                          const int64_t* __restrict__ band_end = nullptr) {
     __shared__ long long s_item;
-    if (threadIdx.x == 0) s_item = (long long)atomicAdd(ticket, 1ull);
+    if (threadIdx.x == 0) {
+        long long x = item_lo + (long long)atomicAdd(ticket, 1ull);
+        if (rev_bands > 0 && x < item_hi) {
+            const long long y = item_hi - x;  // in [1, item_hi]
+            int lo = 0, hi = rev_bands - 1;   // first band whose end is >= y
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (band_end[mid] >= y) hi = mid; else lo = mid + 1;
+            }
+            const long long bs = lo > 0 ? band_end[lo - 1] : 0;
+            x = bs + (x - (item_hi - band_end[lo]));
+        }
+        s_item = x;
+    }
     __syncthreads();
     const int64_t item = s_item;
-    if (item >= nitems) return false;
+    if (item >= item_hi) return false;
     if (threadIdx.x == 0) {
         int lo = 0, hi = tilem;
         while (hi - lo > 1) {
@@ -128,6 +149,7 @@ __device__ bool next_item(unsigned long long* ticket, const int64_t* __restrict_
         const int64_t q = item - item_prefix[lo];
         const int64_t nreg = item_prefix[lo + 1] - item_prefix[lo];
         const int64_t ts = tile_ptrC[lo], ntc = tile_ptrC[lo + 1] - ts;
+        s_it->id = item;
         s_it->i = lo;
         s_it->q = (int)q;
         s_it->rs = (int)(ts + (q * ntc) / nreg);
@@ -413,7 +435,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
     __shared__ int s_fx;
     const int tid = threadIdx.x;
 
-    while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
+    while (next_item(ticket, item_prefix, tilem, 0, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
         const Cursors cu = it.na <= MAXA_SMEM ? cursors_at(cur_s, MAXA_SMEM)
                                               : cursors_at(cursor_g + (int64_t)blockIdx.x * 4 * max_na, max_na);
@@ -479,13 +501,16 @@ __device__ __forceinline__ void acc_add(ACC* a, ACC v) { atomicAdd(a, v); }
 
 template <typename V, typename ACC>
 __global__ void __launch_bounds__(RW_THREADS, sizeof(ACC) == 4 ? 2 : 1)
-rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t nitems,
+rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t item_lo,
+                  int64_t item_hi,
                   const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                   const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
                   const uint8_t* __restrict__ ptrRowC, const int* __restrict__ a_rp, const int* __restrict__ a_ci,
                   const V* __restrict__ a_val, const int* __restrict__ b_rp, const int* __restrict__ b_ci,
                   const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
-                  unsigned long long* ticket, int* __restrict__ cursor_g, int max_na) {
+                  unsigned long long* ticket, int* __restrict__ cursor_g, int max_na, int nbands,
+                  const int64_t* __restrict__ band_end, unsigned* __restrict__ band_cnt,
+                  volatile int* band_flag, int band_rev) {
     extern __shared__ __align__(16) uint32_t smem[];
     constexpr int ARENA = nw_arena<ACC>();
     uint2* tinfo = reinterpret_cast<uint2*>(smem);                             // [ntw], then rows, then acc
@@ -497,7 +522,8 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
     __shared__ int s_nt, s_fx, s_nrow;
     const int tid = threadIdx.x;
 
-    while (next_item(ticket, item_prefix, tilem, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
+    while (next_item(ticket, item_prefix, tilem, item_lo, item_hi, tile_ptrC, a_rp, m, &s_it, s_rows,
+                     band_rev ? nbands : 0, band_end)) {
         const ItemInfo it = s_it;
         const Cursors cu = it.na <= MAXA_SMEM ? cursors_at(cur_s, MAXA_SMEM)
                                               : cursors_at(cursor_g + (int64_t)blockIdx.x * 4 * max_na, max_na);
@@ -597,6 +623,36 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             __syncthreads();
             t0 = t1;
         }
+        if (nbands > 0) {
+            // band accounting: every thread's stores of this item are made
+            // visible system-wide, then the item counts down its band; the
+            // item that completes the band raises the band's host flag
+            __threadfence_system();
+            __syncthreads();
+            if (tid == 0) {
+                int lo = 0, hi = nbands - 1;  // first band whose item end is > id
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (band_end[mid] > it.id) hi = mid; else lo = mid + 1;
+                }
+                const int64_t start = lo > 0 ? band_end[lo - 1] : 0;
+                const unsigned done = atomicAdd(&band_cnt[lo], 1u) + 1u;
+                if ((int64_t)done == band_end[lo] - start) {
+                    __threadfence_system();
+                    band_flag[lo] = 1;
+                }
+            }
+        }
+    }
+}
+
+// band_end[k] = first work item after band k (band k = tile-rows
+// [rows[k], rows[k+1])); band counters cleared.
+__global__ void band_plan_kernel(int nbands, const int* __restrict__ rows, const int64_t* __restrict__ item_prefix,
+                                 int64_t* __restrict__ band_end, unsigned* __restrict__ band_cnt) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nbands; k += gridDim.x * blockDim.x) {
+        band_end[k] = item_prefix[rows[k + 1]];
+        band_cnt[k] = 0u;
     }
 }
 
@@ -684,9 +740,18 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     return SPG_OK;
 }
 
+// Band reporting of one numeric launch (nbands == 0: none).
+struct BandArgs {
+    int nbands = 0;
+    const int64_t* band_end = nullptr;
+    unsigned* band_cnt = nullptr;
+    volatile int* band_flag = nullptr;
+    int rev = 0;  // bands dispatched from the last to the first
+};
+
 template <typename V, typename ACC>
 static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                                 RowwisePriv* rp) {
+                                 RowwisePriv* rp, int64_t item_lo, int64_t item_hi, const BandArgs& ba) {
     const int nwords_b = (B->tilen + 31) / 32;
     const size_t smem = num_smem<ACC>(nwords_b);
     if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: B too wide");
@@ -697,20 +762,52 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
     SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_numeric_kernel<V, ACC>, RW_THREADS, smem));
     const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
     rw_numeric_kernel<V, ACC><<<grid, RW_THREADS, smem, h->stream>>>(
-        A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
+        A->m, nwords_b, rp->item_prefix, C->tilem, item_lo, item_hi, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
-        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na);
+        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na,
+        ba.nbands, ba.band_end, ba.band_cnt, ba.band_flag, ba.rev);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }
 
 spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
-                           spg_precision prec) {
+                           spg_precision prec, int r0, int r1) {
     if (C->numtileC == 0 || C->nnzC == 0) return SPG_OK;
     SPG_TRY(rw_prepare(h, A, B, C, rp));
-    if (A->dtype == SPG_F64) return launch_numeric<double, double>(h, A, B, C, rp);
-    if (prec == SPG_PREC_F64) return launch_numeric<float, double>(h, A, B, C, rp);
-    return launch_numeric<float, float>(h, A, B, C, rp);
+    // the items of tile-rows [r0, r1); the whole range needs no device read
+    // (the batch path captures this launch into CUDA graphs)
+    int64_t lo = 0, hi = rp->nitems;
+    if (r1 < 0) r1 = C->tilem;
+    if (r0 > 0) SPG_TRY(spg_read_i64(h, rp->item_prefix + r0, &lo));
+    if (r1 < C->tilem) SPG_TRY(spg_read_i64(h, rp->item_prefix + r1, &hi));
+    if (hi <= lo) return SPG_OK;
+    const BandArgs none{};
+    if (A->dtype == SPG_F64) return launch_numeric<double, double>(h, A, B, C, rp, lo, hi, none);
+    if (prec == SPG_PREC_F64) return launch_numeric<float, double>(h, A, B, C, rp, lo, hi, none);
+    return launch_numeric<float, float>(h, A, B, C, rp, lo, hi, none);
+}
+
+spg_status rowwise_numeric_bands_launch(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                                        RowwisePriv* rp, spg_precision prec, int nbands, const int* d_rows,
+                                        int64_t* d_band_end, unsigned* d_band_cnt, volatile int* band_flag_dev,
+                                        int64_t* h_band_end, bool last_first) {
+    SPG_TRY(rw_prepare(h, A, B, C, rp));
+    band_plan_kernel<<<(nbands + 255) / 256, 256, 0, h->stream>>>(nbands, d_rows, rp->item_prefix, d_band_end,
+                                                                  d_band_cnt);
+    SPG_CUDA(h, cudaGetLastError());
+    SPG_CUDA(h, cudaMemcpyAsync(h_band_end, d_band_end, (size_t)nbands * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                h->stream));
+    SPG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (C->numtileC == 0 || C->nnzC == 0 || rp->nitems == 0) return SPG_OK;
+    BandArgs ba;
+    ba.nbands = nbands;
+    ba.band_end = d_band_end;
+    ba.band_cnt = d_band_cnt;
+    ba.band_flag = band_flag_dev;
+    ba.rev = last_first ? 1 : 0;
+    if (A->dtype == SPG_F64) return launch_numeric<double, double>(h, A, B, C, rp, 0, rp->nitems, ba);
+    if (prec == SPG_PREC_F64) return launch_numeric<float, double>(h, A, B, C, rp, 0, rp->nitems, ba);
+    return launch_numeric<float, float>(h, A, B, C, rp, 0, rp->nitems, ba);
 }
 
 // Numeric launch only (no host synchronisation once the plan exists): the

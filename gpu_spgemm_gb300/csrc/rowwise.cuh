@@ -15,7 +15,19 @@ struct RowwisePriv {
 spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B);
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                             RowwisePriv* rp, int64_t* tile_cnt);
+// Numeric phase on C tile-rows [r0, r1) (r1 < 0: every tile-row).
 spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                           RowwisePriv* rp, spg_precision prec);
+                           RowwisePriv* rp, spg_precision prec, int r0 = 0, int r1 = -1);
+// One numeric launch over every tile-row that reports bands of tile-rows as
+// they complete: band k = tile-rows [rows[k], rows[k+1]) (d_rows on the
+// device, nbands + 1 entries).  Fills h_band_end[k] (first work item after
+// band k; host memory) before the launch; the kernel sets band_flag[k] (a
+// device pointer to mapped host memory, cleared by the caller) when every
+// item of band k is written.  last_first: work items are taken from the
+// last band to the first.  Returns after the launch without waiting.
+spg_status rowwise_numeric_bands_launch(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
+                                        RowwisePriv* rp, spg_precision prec, int nbands, const int* d_rows,
+                                        int64_t* d_band_end, unsigned* d_band_cnt, volatile int* band_flag_dev,
+                                        int64_t* h_band_end, bool last_first);
 void rowwise_free_priv(spg_handle_t h, RowwisePriv* rp);
 void rowwise_free_bview(spg_handle_t h, spg_tiles* t);

@@ -9,8 +9,12 @@
 // status codes.
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
+#include <chrono>
 #include <cstring>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "plain.cuh"
 #include "rowwise.cuh"
@@ -125,6 +129,7 @@ extern "C" spg_status spg_destroy(spg_handle_t h) {
     for (auto& ev : h->ev) cudaEventDestroy(ev);
     cudaFree(h->d_flags);
     cudaFreeHost(h->h_pinned);
+    if (h->h_band) cudaFreeHost(h->h_band);
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, h->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
     delete h;
@@ -373,28 +378,155 @@ extern "C" spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, con
     return s;
 }
 
-extern "C" spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
-                                  spg_precision prec, spg_ctiles* C) {
+// Step 3 on C tile-rows [r0, r1).
+static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                               spg_precision prec, spg_ctiles* C, int r0, int r1) {
     SPG_TRY(validate_pair(h, A, B, C));
     if (!C->priv) return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic structure");
     if (C->numtileC > 0 && (!C->maskC || !C->tile_nnzC || !C->tile_valC))
         return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
+    if (r0 < 0 || r1 < r0 || r1 > C->tilem) return spg_fail(h, SPG_ERR_INVALID, "numeric: bad tile-row range");
     CPriv* cp = static_cast<CPriv*>(C->priv);
     if (algo == SPG_ALGO_AUTO) algo = cp->algo;
     if (algo == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) algo = SPG_ALGO_PLAIN;
+    const bool whole = r0 == 0 && r1 == C->tilem;
     SPG_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
-    if (prec == SPG_PREC_MIXED && A->dtype == SPG_F32) {
-        // dense tile pairs on tensor cores (plain per-C-tile structure)
-        SPG_TRY(plain_step3_mixed(h, A, B, C, &cp->plain, h->dense_thr, h->cancel_eps));
-    } else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32)) {
-        SPG_TRY(rowwise_numeric(h, A, B, C, &cp->rw, prec));
+    const bool mixed = prec == SPG_PREC_MIXED && A->dtype == SPG_F32;
+    if (!mixed && (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32))) {
+        SPG_TRY(rowwise_numeric(h, A, B, C, &cp->rw, prec, r0, r1));
     } else {
-        SPG_TRY(plain_step3(h, A, B, C, &cp->plain));
+        int64_t t0 = 0, t1 = C->numtileC;  // C tiles of the tile-rows
+        if (!whole) {
+            int x0 = 0, x1 = 0;
+            SPG_TRY(spg_read_i32(h, C->tile_ptrC + r0, &x0));
+            SPG_TRY(spg_read_i32(h, C->tile_ptrC + r1, &x1));
+            t0 = x0;
+            t1 = x1;
+        }
+        if (mixed)  // dense tile pairs on tensor cores (plain per-C-tile structure)
+            SPG_TRY(plain_step3_mixed(h, A, B, C, &cp->plain, h->dense_thr, h->cancel_eps, t0, t1));
+        else
+            SPG_TRY(plain_step3(h, A, B, C, &cp->plain, t0, t1));
     }
     SPG_CUDA(h, cudaEventRecord(h->ev[4], h->stream));
     SPG_CUDA(h, cudaEventSynchronize(h->ev[4]));
     h->stats.ms_step3 = elapsed(h, 3, 4);
     return spg_check_flags(h, "numeric");
+}
+
+extern "C" spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                                  spg_precision prec, spg_ctiles* C) {
+    if (!h || !C) return SPG_ERR_INVALID;
+    return numeric_impl(h, A, B, algo, prec, C, 0, C->tilem);
+}
+
+// spg_numeric that reports bands of tile-rows as they complete.  Row-wise:
+// one launch; its work items count down per band and the item completing a
+// band sets the band's flag in mapped host memory, which this thread polls
+// (sleeping between polls, bounded by the stream finishing or a time limit).
+// Plain and mixed: one launch per band, reported in order.
+extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                                        spg_precision prec, spg_ctiles* C, int nbands, const int* band_rows,
+                                        int order, spg_band_fn fn, void* user) {
+    if (!h || !C) return SPG_ERR_INVALID;
+    SPG_TRY(validate_pair(h, A, B, C));
+    if (nbands < 1 || nbands > (1 << 16) || !band_rows || !fn ||
+        (order != SPG_BANDS_FIRST_TO_LAST && order != SPG_BANDS_LAST_TO_FIRST))
+        return spg_fail(h, SPG_ERR_INVALID, "numeric bands: 1..65536 bands, row bounds, an order and a callback");
+    const bool last_first = order == SPG_BANDS_LAST_TO_FIRST;
+    if (band_rows[0] != 0 || band_rows[nbands] != C->tilem)
+        return spg_fail(h, SPG_ERR_INVALID, "numeric bands: bounds must run from 0 to tilem");
+    for (int k = 0; k < nbands; k++)
+        if (band_rows[k + 1] < band_rows[k]) return spg_fail(h, SPG_ERR_INVALID, "numeric bands: bounds descend");
+    if (!C->priv) return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic structure");
+    if (C->numtileC > 0 && (!C->maskC || !C->tile_nnzC || !C->tile_valC))
+        return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
+    CPriv* cp = static_cast<CPriv*>(C->priv);
+    spg_algo a = algo == SPG_ALGO_AUTO ? cp->algo : algo;
+    if (a == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) a = SPG_ALGO_PLAIN;
+    const bool mixed = prec == SPG_PREC_MIXED && A->dtype == SPG_F32;
+    const bool rowwise = !mixed && (a == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32));
+    if (!rowwise) {
+        float ms = 0.f;
+        for (int j = 0; j < nbands; j++) {
+            const int k = last_first ? nbands - 1 - j : j;
+            SPG_TRY(numeric_impl(h, A, B, algo, prec, C, band_rows[k], band_rows[k + 1]));
+            ms += h->stats.ms_step3;
+            fn(user, k, band_rows[k], band_rows[k + 1]);
+        }
+        h->stats.ms_step3 = ms;
+        return SPG_OK;
+    }
+    if (h->band_cap < nbands) {
+        if (h->h_band) cudaFreeHost(h->h_band);
+        h->h_band = nullptr;
+        h->d_band = nullptr;
+        h->band_cap = 0;
+        SPG_CUDA(h, cudaHostAlloc(reinterpret_cast<void**>(&h->h_band), (size_t)nbands * sizeof(int),
+                                  cudaHostAllocMapped));
+        SPG_CUDA(h, cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->d_band), h->h_band, 0));
+        h->band_cap = nbands;
+    }
+    volatile int* flag = h->h_band;
+    for (int k = 0; k < nbands; k++) flag[k] = 0;
+    int* d_rows = nullptr;
+    int64_t* d_end = nullptr;
+    unsigned* d_cnt = nullptr;
+    SPG_TRY(spg_alloc_t(h, &d_rows, (size_t)nbands + 1));
+    SPG_TRY(spg_alloc_t(h, &d_end, (size_t)nbands));
+    SPG_TRY(spg_alloc_t(h, &d_cnt, (size_t)nbands));
+    SPG_CUDA(h, cudaMemcpyAsync(d_rows, band_rows, ((size_t)nbands + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                                h->stream));
+    std::vector<int64_t> end((size_t)nbands);
+    SPG_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
+    const spg_status ls = rowwise_numeric_bands_launch(h, A, B, C, &cp->rw, prec, nbands, d_rows, d_end, d_cnt,
+                                                       h->d_band, end.data(), last_first);
+    if (ls != SPG_OK) return ls;
+    SPG_CUDA(h, cudaEventRecord(h->ev[4], h->stream));
+    std::vector<char> told((size_t)nbands, 0);
+    int left = nbands;
+    for (int k = 0; k < nbands; k++)  // bands without work items are complete now
+        if (end[k] == (k ? end[k - 1] : 0) || C->nnzC == 0) {
+            told[k] = 1;
+            left--;
+            fn(user, k, band_rows[k], band_rows[k + 1]);
+        }
+    const auto t_start = std::chrono::steady_clock::now();
+    bool finished = false;
+    while (left > 0) {
+        bool any = false;
+        for (int k = 0; k < nbands; k++)
+            if (!told[k] && flag[k]) {
+                std::atomic_thread_fence(std::memory_order_acquire);
+                told[k] = 1;
+                left--;
+                any = true;
+                fn(user, k, band_rows[k], band_rows[k + 1]);
+            }
+        if (left == 0 || any) continue;
+        if (finished) return spg_fail(h, SPG_ERR_CUDA, "numeric bands: launch ended with bands unreported");
+        const cudaError_t q = cudaEventQuery(h->ev[4]);
+        if (q == cudaSuccess) {
+            finished = true;  // every flag store is visible now: one more scan
+            continue;
+        }
+        if (q != cudaErrorNotReady) return spg_cuda_fail(h, q, "numeric bands");
+        if (std::chrono::steady_clock::now() - t_start > std::chrono::seconds(600))
+            return spg_fail(h, SPG_ERR_TIMEOUT, "numeric bands: no completion within 600 s");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    SPG_CUDA(h, cudaEventSynchronize(h->ev[4]));
+    spg_free_async(h, d_rows);
+    spg_free_async(h, d_end);
+    spg_free_async(h, d_cnt);
+    h->stats.ms_step3 = elapsed(h, 3, 4);
+    return spg_check_flags(h, "numeric bands");
+}
+
+extern "C" spg_status spg_numeric_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                                       spg_precision prec, spg_ctiles* C, int row_begin, int row_end) {
+    if (!h || !C) return SPG_ERR_INVALID;
+    return numeric_impl(h, A, B, algo, prec, C, row_begin, row_end);
 }
 
 extern "C" spg_status spg_spgemm(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,

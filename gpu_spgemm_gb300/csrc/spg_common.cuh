@@ -81,6 +81,9 @@ struct spg_handle_s {
     spg_stats stats{};
     unsigned* d_flags = nullptr;      // device error bits
     int64_t* h_pinned = nullptr;      // 64 pinned words for read-backs
+    int* h_band = nullptr;            // mapped pinned band flags (spg_numeric_bands), band_cap entries
+    int* d_band = nullptr;            // the same flags' device address
+    int band_cap = 0;
     cudaEvent_t ev[8]{};
     int num_sms = 0;
     size_t smem_optin = 0;

@@ -198,6 +198,36 @@ spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, const spg_tile
 spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                        spg_precision prec, spg_ctiles* C);
 
+/* spg_numeric on the C tile-rows [row_begin, row_end) only (0 <= row_begin <=
+ * row_end <= C->tilem): the values and column bytes of tiles tile_ptrC[row_begin]
+ * .. tile_ptrC[row_end] - 1.  Calls over bands that cover every tile-row once
+ * give what one spg_numeric gives, so a caller can copy a finished band to the
+ * host while the next band computes.  Same step of the reference as
+ * spg_numeric. */
+spg_status spg_numeric_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                            spg_precision prec, spg_ctiles* C, int row_begin, int row_end);
+
+/* spg_numeric that reports its progress in bands of C tile-rows: band k is
+ * tile-rows [band_rows[k], band_rows[k+1]) (band_rows: nbands + 1 ascending
+ * bounds from 0 to C->tilem, 1 <= nbands <= 65536).  order says which bands
+ * are worked on first: SPG_BANDS_FIRST_TO_LAST, or SPG_BANDS_LAST_TO_FIRST
+ * (when the first tile-rows hold most of the work, as the hub rows of a
+ * power-law matrix do, the other bands' results are then ready early and can
+ * be copied while the heavy band computes).  fn(user, k, row_begin,
+ * row_end) is called on the calling thread once per band, as soon as the
+ * values and column bytes of that band's tiles are final in device memory
+ * (bands may complete out of order; a band without work is reported at
+ * once).  The call returns when the whole phase has finished.  fn may
+ * enqueue copies of the finished band on other streams or handles; it must
+ * not call into this handle.  The row-wise path runs one launch whose work
+ * items count down per band; the plain and mixed paths run one launch per
+ * band.  Same step of the reference as spg_numeric. */
+typedef void (*spg_band_fn)(void* user, int band, int row_begin, int row_end);
+enum { SPG_BANDS_FIRST_TO_LAST = 0, SPG_BANDS_LAST_TO_FIRST = 1 };
+spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                             spg_precision prec, spg_ctiles* C, int nbands, const int* band_rows, int order,
+                             spg_band_fn fn, void* user);
+
 /* Steps 1-3 in one call (the timed region of src/spgemm_raw_v2.cu:115-240). */
 spg_status spg_spgemm(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                       spg_precision prec, spg_ctiles* C);

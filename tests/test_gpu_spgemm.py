@@ -247,3 +247,90 @@ def test_split_symbolic_matches_one_call(handle, algo):
     for k in STRUCT_KEYS:
         np.testing.assert_array_equal(got[k], S[k].astype(got[k].dtype), err_msg=k)
     assert rel_frob(got["tile_valC"], S["tile_valC"]) <= TOL[np.float32]
+
+
+@pytest.mark.parametrize("algo,prec,name,a", [
+    ("rowwise", "f32", "rmat_12", synth.rmat(12, 16)),
+    ("plain", "f32", "rmat_12", synth.rmat(12, 16)),
+    ("rowwise", "f64", "rmat_11", synth.rmat(11, 16)),
+    ("plain", "mixed", "stencil27_6", synth.stencil27_dof3(6)),
+], ids=["rowwise-f32", "plain-f32", "rowwise-f64acc", "plain-mixed"])
+def test_numeric_rows_bands_match_whole(handle, algo, prec, name, a):
+    """spg_numeric_rows over uneven tile-row bands (one of them empty) gives
+    the product one spg_numeric gives; bad ranges are refused."""
+    from gpu_spgemm_gb300 import _lib as L
+    a = a.astype(np.float32)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    S = oracle.spgemm_tiles(a, a)
+    Cm = api.symbolic(handle, A, B, algo=algo)
+    tm = Cm.tilem
+    for bad in ((-1, 1), (2, 1), (0, tm + 1)):
+        with pytest.raises(L.SpgError):
+            api.numeric_rows(handle, A, B, Cm, *bad, algo=algo, prec=prec)
+    bounds = [0, 1, 1, max(2, tm // 3), max(3, (3 * tm) // 4), tm]
+    for r0, r1 in zip(bounds[:-1], bounds[1:]):
+        api.numeric_rows(handle, A, B, Cm, r0, r1, algo=algo, prec=prec)
+    got = Cm.to_host()
+    for k in STRUCT_KEYS:
+        np.testing.assert_array_equal(got[k], S[k].astype(got[k].dtype), err_msg=k)
+    tol = 1e-7 if prec == "f64" else TOL[np.float32]
+    assert rel_frob(got["tile_valC"], S["tile_valC"]) <= tol
+
+
+@pytest.mark.parametrize("algo,prec,a", [
+    ("rowwise", "f32", synth.rmat(13, 16)),
+    ("rowwise", "f64", synth.rmat(11, 16)),
+    ("plain", "f32", synth.rmat(11, 16)),
+    ("plain", "mixed", synth.stencil27_dof3(6)),
+], ids=["rowwise-f32", "rowwise-f64acc", "plain-f32", "plain-mixed"])
+@pytest.mark.parametrize("last_first", [False, True], ids=["first-to-last", "last-to-first"])
+def test_numeric_bands_report_final_values(handle, algo, prec, a, last_first):
+    """spg_numeric_bands reports every band once, and a band's values and
+    column bytes, copied by a second handle on another stream inside the
+    callback (while the numeric launch may still run), already match the
+    oracle.  Bad band bounds are refused."""
+    import ctypes as C
+    import torch
+    from gpu_spgemm_gb300 import _lib as L
+    a = a.astype(np.float32)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    S = oracle.spgemm_tiles(a, a)
+    Cm = api.symbolic(handle, A, B, algo=algo)
+    tm = Cm.tilem
+    tp, pre = S["tile_ptrC"], S["tile_nnzC"]
+    for bad in ([1, tm], [0, tm - 1], [0, 3, 2, tm]):
+        with pytest.raises(L.SpgError):
+            api.numeric_bands(handle, A, B, Cm, bad, lambda *x: None, algo=algo, prec=prec)
+    rows_ok = np.array([0, tm], np.int32)
+    assert handle.lib.spg_numeric_bands(handle.h, C.byref(A.t), C.byref(B.t), api._ALGOS[algo], api._PRECS[prec],
+                                        C.byref(Cm.c), 1, rows_ok.ctypes.data, 2, L.BAND_FN(lambda *x: None),
+                                        None) == L.SPG_ERR_INVALID
+    bounds = sorted({0, 1, tm // 5, tm // 2, (4 * tm) // 5, tm}) + [tm]  # the last band is empty
+    side = api.Handle(0, torch.cuda.Stream())
+    seen = []
+    P = lambda x: x.ctypes.data_as(C.c_void_p)
+    try:
+        def on_band(k, r0, r1):
+            t0, t1 = int(tp[r0]), int(tp[r1])
+            v0, v1 = int(pre[t0]), int(pre[t1])
+            v = np.zeros(max(1, v1 - v0), np.float32)
+            cc = np.zeros(max(1, v1 - v0), np.uint8)
+            nv = C.c_int64()
+            side.check(side.lib.spg_ctiles_to_host_range(side.h, C.byref(Cm.c), t0, t1, None, None, None, None,
+                                                         None, P(v), P(cc), v.size, C.byref(nv)))
+            assert nv.value == v1 - v0
+            seen.append((k, r0, r1, rel_frob(v[:v1 - v0], S["tile_valC"][v0:v1]),
+                         bool(np.array_equal(cc[:v1 - v0], S["tile_colC"][v0:v1]))))
+
+        api.numeric_bands(handle, A, B, Cm, bounds, on_band, algo=algo, prec=prec, last_first=last_first)
+    finally:
+        side.close()
+    assert sorted(s[0] for s in seen) == list(range(len(bounds) - 1))
+    for k, r0, r1, err, cols in seen:
+        assert (r0, r1) == (bounds[k], bounds[k + 1])
+        assert cols, k
+        assert err <= (1e-7 if prec == "f64" else TOL[np.float32]), (k, err)
+    got = Cm.to_host()
+    assert rel_frob(got["tile_valC"], S["tile_valC"]) <= TOL[np.float32]
