@@ -36,9 +36,13 @@ constexpr int RW_WARPS = RW_THREADS / 32;
 constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
 // numeric window arena (bytes): 8 B a tile + 5 B a non-empty tile row +
-// sizeof(ACC) a value
+// sizeof(ACC) a value.  These are the sizes that always fit; a launch grows
+// its arena into whatever shared memory its blocks per SM leave (the rank
+// bitmap is sized by B's width).  Row words keep value offsets in 16 bits, so
+// an arena stays below 2^16 values.
 constexpr int NW_ARENA_F32 = 74752;   // two blocks per SM
 constexpr int NW_ARENA_F64 = 131072;  // one block per SM
+constexpr int NW_ARENA_MAX = 196608;
 template <typename ACC>
 constexpr int nw_arena() { return sizeof(ACC) == 4 ? NW_ARENA_F32 : NW_ARENA_F64; }
 constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose cursors fit in shared memory
@@ -510,9 +514,9 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
                   unsigned long long* ticket, int* __restrict__ cursor_g, int max_na, int nbands,
                   const int64_t* __restrict__ band_end, unsigned* __restrict__ band_cnt,
-                  volatile int* band_flag, int band_rev) {
+                  volatile int* band_flag, int band_rev, int arena) {
     extern __shared__ __align__(16) uint32_t smem[];
-    constexpr int ARENA = nw_arena<ACC>();
+    const int ARENA = arena;  // bytes, a multiple of 16
     uint2* tinfo = reinterpret_cast<uint2*>(smem);                             // [ntw], then rows, then acc
     int* cur_s = reinterpret_cast<int*>(reinterpret_cast<char*>(smem) + ARENA); // 4 x MAXA_SMEM
     uint2* bp = reinterpret_cast<uint2*>(cur_s + 4 * MAXA_SMEM);               // nwords_b
@@ -753,8 +757,36 @@ template <typename V, typename ACC>
 static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                                  RowwisePriv* rp, int64_t item_lo, int64_t item_hi, const BandArgs& ba) {
     const int nwords_b = (B->tilen + 31) / 32;
-    const size_t smem = num_smem<ACC>(nwords_b);
+    size_t smem = num_smem<ACC>(nwords_b);
     if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: B too wide");
+    // grow the arena into the shared memory left at the blocks per SM the
+    // registers allow (two for FP32 accumulators, one for FP64); keep the
+    // fixed size if the occupancy query disagrees
+    int arena = nw_arena<ACC>();
+    {
+        const int target = sizeof(ACC) == 4 ? 2 : 1;
+        cudaFuncAttributes fa{};
+        SPG_CUDA(h, cudaFuncGetAttributes(&fa, rw_numeric_kernel<V, ACC>));
+        const size_t fixed = smem - (size_t)arena + fa.sharedSizeBytes + 1024;  // + per-block reservation
+        size_t per_block = h->smem_per_sm / target;
+        if (per_block > h->smem_optin + 1024) per_block = h->smem_optin + 1024;
+        if (per_block > fixed) {
+            size_t cand = (per_block - fixed) & ~(size_t)15;
+            if (cand > (size_t)NW_ARENA_MAX) cand = NW_ARENA_MAX;
+            if (cand > (size_t)arena) {
+                const size_t s2 = smem - (size_t)arena + cand;
+                SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<V, ACC>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+                int o2 = 0;
+                SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, rw_numeric_kernel<V, ACC>,
+                                                                          RW_THREADS, s2));
+                if (o2 >= target) {
+                    arena = (int)cand;
+                    smem = s2;
+                }
+            }
+        }
+    }
     SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<V, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters + 1, 0, sizeof(unsigned long long), h->stream));
@@ -765,7 +797,7 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
         A->m, nwords_b, rp->item_prefix, C->tilem, item_lo, item_hi, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
         (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na,
-        ba.nbands, ba.band_end, ba.band_cnt, ba.band_flag, ba.rev);
+        ba.nbands, ba.band_end, ba.band_cnt, ba.band_flag, ba.rev, arena);
     SPG_CUDA(h, cudaGetLastError());
     return SPG_OK;
 }

@@ -105,6 +105,7 @@ extern "C" spg_status spg_create(spg_handle_t* out, int device, void* stream) {
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { delete h; return SPG_ERR_CUDA; }
     h->num_sms = prop.multiProcessorCount;
     h->smem_optin = prop.sharedMemPerBlockOptin;
+    h->smem_per_sm = prop.sharedMemPerMultiprocessor;
     if (cudaMalloc(&h->d_flags, 256) != cudaSuccess) { delete h; return SPG_ERR_OOM; }
     cudaMemset(h->d_flags, 0, 256);
     if (cudaMallocHost(&h->h_pinned, 64 * sizeof(int64_t)) != cudaSuccess) {

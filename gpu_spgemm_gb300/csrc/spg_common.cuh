@@ -87,6 +87,7 @@ struct spg_handle_s {
     cudaEvent_t ev[8]{};
     int num_sms = 0;
     size_t smem_optin = 0;
+    size_t smem_per_sm = 0;
 };
 
 spg_status spg_fail(spg_handle_t h, spg_status s, const std::string& msg);
