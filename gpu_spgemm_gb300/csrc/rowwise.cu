@@ -36,10 +36,10 @@ constexpr int RW_WARPS = RW_THREADS / 32;
 constexpr int RT = 16384;       // C tiles per work item
 constexpr int WS = 2048;        // C tiles per symbolic window
 // numeric window arena (bytes): 8 B a tile + 5 B a non-empty tile row +
-// sizeof(ACC) a value.  These are the sizes that always fit; a launch grows
-// its arena into whatever shared memory its blocks per SM leave (the rank
-// bitmap is sized by B's width).  Row words keep value offsets in 16 bits, so
-// an arena stays below 2^16 values.
+// sizeof(ACC) a value + 8 B per 32 tile columns the window spans (its rank
+// bitmap).  These are the sizes that always fit; a launch grows its arena
+// into whatever shared memory its blocks per SM leave.  Row words keep value
+// offsets in 16 bits, so an arena stays below 2^16 values.
 constexpr int NW_ARENA_F32 = 74752;   // two blocks per SM
 constexpr int NW_ARENA_F64 = 131072;  // one block per SM
 constexpr int NW_ARENA_MAX = 196608;
@@ -505,7 +505,7 @@ __device__ __forceinline__ void acc_add(ACC* a, ACC v) { atomicAdd(a, v); }
 
 template <typename V, typename ACC>
 __global__ void __launch_bounds__(RW_THREADS, sizeof(ACC) == 4 ? 2 : 1)
-rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, int tilem, int64_t item_lo,
+rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int64_t item_lo,
                   int64_t item_hi,
                   const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                   const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
@@ -517,9 +517,8 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
                   volatile int* band_flag, int band_rev, int arena) {
     extern __shared__ __align__(16) uint32_t smem[];
     const int ARENA = arena;  // bytes, a multiple of 16
-    uint2* tinfo = reinterpret_cast<uint2*>(smem);                             // [ntw], then rows, then acc
+    uint2* tinfo = reinterpret_cast<uint2*>(smem);  // [ntw], then rows, acc and the rank bitmap
     int* cur_s = reinterpret_cast<int*>(reinterpret_cast<char*>(smem) + ARENA); // 4 x MAXA_SMEM
-    uint2* bp = reinterpret_cast<uint2*>(cur_s + 4 * MAXA_SMEM);               // nwords_b
     __shared__ ItemInfo s_it;
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
@@ -536,15 +535,18 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
         while (t0 < it.re) {
             // window [t0, t1): the longest run of n tiles whose metadata (8 B
             // a tile, 5 B a non-empty row: at most min(values, 16 a tile)),
-            // values and 16 B of alignment slack fit the arena (one tile
-            // always fits).  fits(n) is monotone: one sample per thread, then
-            // the bracket after the last fitting sample.
+            // values, rank bitmap (8 B per 32 tile columns spanned) and 32 B
+            // of alignment slack fit the arena (one tile always fits).
+            // fits(n) is monotone (the tile-row's columns ascend): one sample
+            // per thread, then the bracket after the last fitting sample.
             const int64_t v0 = tile_nnzC[t0];
+            const int wlo0 = colidxC[t0] >> 5;
             const int cap_t = min(ARENA / 8, it.re - t0);
             auto fits = [&](int n) {
                 const int64_t nvx = tile_nnzC[t0 + n] - v0;
                 const int64_t rb = nvx < 16 * (int64_t)n ? nvx : 16 * (int64_t)n;
-                return 8 * (int64_t)n + 5 * rb + (int64_t)sizeof(ACC) * nvx + 16 <= ARENA;
+                const int64_t nwdx = (int64_t)((colidxC[t0 + n - 1] >> 5) - wlo0 + 1);
+                return 8 * (int64_t)n + 5 * rb + (int64_t)sizeof(ACC) * nvx + 8 * nwdx + 32 <= ARENA;
             };
             const int step = (cap_t + RW_THREADS - 1) / RW_THREADS;
             if (tid == 0) { s_nt = 0; s_nrow = 0; }
@@ -576,6 +578,8 @@ rw_numeric_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix, 
             uint8_t* rowr = reinterpret_cast<uint8_t*>(rows + rcap);  // each row word's row in its tile
             const size_t aoff = ((size_t)(rowr + rcap - reinterpret_cast<uint8_t*>(smem)) + 15) & ~(size_t)15;
             ACC* acc = reinterpret_cast<ACC*>(reinterpret_cast<uint8_t*>(smem) + aoff);  // 16-byte aligned
+            const size_t boff = (aoff + sizeof(ACC) * (size_t)nv + 7) & ~(size_t)7;
+            uint2* bp = reinterpret_cast<uint2*>(reinterpret_cast<uint8_t*>(smem) + boff);  // nwd words
             // tile and row words, one thread per tile: 2 x 16 B of masks, 16 B
             // of row offsets and the tile's value offset, all loads in flight;
             // the tile's non-empty rows get a block of row words from a counter
@@ -665,8 +669,8 @@ size_t sym_smem(int nwords_b) {
 }
 
 template <typename ACC>
-size_t num_smem(int nwords_b) {
-    return (size_t)nw_arena<ACC>() + (size_t)MAXA_SMEM * 16 + (size_t)nwords_b * 8;
+size_t num_smem() {
+    return (size_t)nw_arena<ACC>() + (size_t)MAXA_SMEM * 16;
 }
 
 }  // namespace
@@ -680,7 +684,7 @@ size_t num_smem(int nwords_b) {
 // 0.40 ms vs row-wise 0.47 ms.
 spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B) {
     const int nwords_b = (B->tilen + 31) / 32;
-    if (num_smem<double>(nwords_b) > h->smem_optin) return SPG_ALGO_PLAIN;
+    if (sym_smem(nwords_b) > h->smem_optin || num_smem<double>() > h->smem_optin) return SPG_ALGO_PLAIN;
     const double fill = A->numtile > 0 ? (double)A->nnz / (double)A->numtile : 0.0;
     return fill < 6.0 ? SPG_ALGO_ROWWISE : SPG_ALGO_PLAIN;
 }
@@ -756,9 +760,8 @@ struct BandArgs {
 template <typename V, typename ACC>
 static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                                  RowwisePriv* rp, int64_t item_lo, int64_t item_hi, const BandArgs& ba) {
-    const int nwords_b = (B->tilen + 31) / 32;
-    size_t smem = num_smem<ACC>(nwords_b);
-    if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: B too wide");
+    size_t smem = num_smem<ACC>();
+    if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: shared memory too small");
     // grow the arena into the shared memory left at the blocks per SM the
     // registers allow (two for FP32 accumulators, one for FP64); keep the
     // fixed size if the occupancy query disagrees
@@ -794,7 +797,7 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
     SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_numeric_kernel<V, ACC>, RW_THREADS, smem));
     const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
     rw_numeric_kernel<V, ACC><<<grid, RW_THREADS, smem, h->stream>>>(
-        A->m, nwords_b, rp->item_prefix, C->tilem, item_lo, item_hi, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
+        A->m, rp->item_prefix, C->tilem, item_lo, item_hi, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
         (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na,
         ba.nbands, ba.band_end, ba.band_cnt, ba.band_flag, ba.rev, arena);

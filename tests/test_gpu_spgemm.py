@@ -334,3 +334,24 @@ def test_numeric_bands_report_final_values(handle, algo, prec, a, last_first):
         assert err <= (1e-7 if prec == "f64" else TOL[np.float32]), (k, err)
     got = Cm.to_host()
     assert rel_frob(got["tile_valC"], S["tile_valC"]) <= TOL[np.float32]
+
+
+def wide_span_case():
+    """A: 256 rows of 64 columns spread over ~1.05 M columns; B: Erdős–Rényi
+    of that size, degree 2.  C's tile-rows span the whole width sparsely
+    (2,056 rank-bitmap words, most C tiles empty), so row-wise windows are
+    bounded by the span they cover rather than by their values."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    n = (1 << 20) + 4096
+    b = synth.erdos_renyi(n, 2.0, rng)
+    m = 256
+    rows = np.repeat(np.arange(m), 64)
+    cols = rng.integers(0, n, size=m * 64)
+    a = synth._assemble(m, n, [rows], [cols], [rng.random(m * 64) * 2 - 1], np.float32)
+    return a, b
+
+
+@pytest.mark.parametrize("algo", ["rowwise", "plain"])
+def test_wide_sparse_span(handle, algo):
+    a, b = wide_span_case()
+    check_product(handle, a, b, algo, np.float32)
