@@ -42,7 +42,7 @@ TS = 16
 # DRAM bytes per launch of the dominant kernel, from one-pass ncu captures of
 # the same bench command (dram__bytes_read.sum + dram__bytes_write.sum), by
 # (workload, step); profiles/traffic_rmat20.md holds the capture.
-MEASURED_TRAFFIC = {("rmat20", "step3"): 279.11e9 + 65.14e9}
+MEASURED_TRAFFIC = {("rmat20", "step3"): 279.02e9 + 65.14e9}
 
 
 def workload(name: str):

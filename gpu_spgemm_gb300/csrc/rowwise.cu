@@ -86,16 +86,18 @@ __global__ void rw_plan_kernel(int tilem, int m, const int* __restrict__ tile_pt
 }
 
 // Plan, pass 2: work items per tile-row.  A tile-row is cut into regions of
-// at most RT C tiles and at most ~PW products, PW = total / (SMs * 64) (at
-// least 2^16): hub tile-rows of a power-law matrix become many balanced
-// items instead of one long one, so no item holds up the end of a launch or
-// of a band of tile-rows.  (Each item re-seeks its A nonzeros' cursors:
-// R-MAT 2^20 gets 140,774 items instead of 139,942 at SMs * 16.)
+// at most RT C tiles and at most ~PW products, PW = total / (SMs * 16)
+// clamped to [2^16, 2^21]: hub tile-rows of a power-law matrix become many
+// balanced items instead of one long one, and no item runs long enough
+// (~2 M products at most) to hold up the end of a launch or of a band of
+// tile-rows.  Finer items cost time: each re-seeks its A nonzeros' cursors
+// (R-MAT 2^16 ran 15 % slower at total / (SMs * 64)).
 __global__ void rw_plan2_kernel(int tilem, int num_sms, const int* __restrict__ tile_ptrC,
                                 const int64_t* __restrict__ prod, const unsigned long long* __restrict__ total,
                                 int64_t* __restrict__ nitems) {
     const unsigned long long tot = *total;
-    unsigned long long pw = tot / ((unsigned long long)num_sms * 64ull);
+    unsigned long long pw = tot / ((unsigned long long)num_sms * 16ull);
+    if (pw > (1ull << 21)) pw = 1ull << 21;
     if (pw < (1ull << 16)) pw = 1ull << 16;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
         const int64_t ntc = tile_ptrC[i + 1] - tile_ptrC[i];
