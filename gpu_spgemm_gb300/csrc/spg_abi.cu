@@ -473,6 +473,17 @@ extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, cons
     int* d_rows = nullptr;
     int64_t* d_end = nullptr;
     unsigned* d_cnt = nullptr;
+    struct Scratch {  // released on every return, stream-ordered after the launch
+        spg_handle_t h;
+        int** a;
+        int64_t** b;
+        unsigned** c;
+        ~Scratch() {
+            spg_free_async(h, *a);
+            spg_free_async(h, *b);
+            spg_free_async(h, *c);
+        }
+    } scratch{h, &d_rows, &d_end, &d_cnt};
     SPG_TRY(spg_alloc_t(h, &d_rows, (size_t)nbands + 1));
     SPG_TRY(spg_alloc_t(h, &d_end, (size_t)nbands));
     SPG_TRY(spg_alloc_t(h, &d_cnt, (size_t)nbands));
@@ -517,9 +528,6 @@ extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, cons
         std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
     SPG_CUDA(h, cudaEventSynchronize(h->ev[4]));
-    spg_free_async(h, d_rows);
-    spg_free_async(h, d_end);
-    spg_free_async(h, d_cnt);
     h->stats.ms_step3 = elapsed(h, 3, 4);
     return spg_check_flags(h, "numeric bands");
 }
