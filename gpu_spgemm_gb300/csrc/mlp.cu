@@ -9,7 +9,7 @@
 // margin), and step 1 builds every tile-row's bitmap ONCE: it counts exactly,
 // writes the tile columns into the slot when they fit, and a compaction copies
 // the slots into C's exact arrays (plain.cu, c1_slot_kernel and
-// c1_compact_kernel).  The exact bitmap count stays the judge: a tile-row that
+// c1_compact_kernel).  The exact bitmap count has the last word: a tile-row that
 // outgrew its slot re-runs the exact fill.  The structure is never
 // approximated.
 //

@@ -2,7 +2,7 @@
 //
 // Drives the steps the reference's main() drives (src/spgemm_raw_v2.cu:101-243):
 // tiling, C tile structure, bitmask symbolic, scans, numeric.  Differences from
-// the reference driver: all work is ordered on one caller-chosen stream, device
+// the reference's host program: all work is ordered on one caller-chosen stream, device
 // memory comes from the stream-ordered pool allocator (the reference's
 // cudaMalloc/cudaFree pairs around each CUB scan disappear), every CUDA call is
 // checked, C's nnz prefix is int64, and device-side error bits are turned into

@@ -10,7 +10,7 @@
  * exactly as csr2tile / build_csc_tiles lay them out.
  *
  * The reference has no library API: its "interface" is the host functions of
- * tile_format.h, the kernel signatures and the driver sequence of
+ * tile_format.h, the kernel signatures and the host call sequence of
  * src/spgemm_raw_v2.cu:101-243.  Each entry point below names the reference code
  * it replaces.
  *
