@@ -401,7 +401,7 @@ def measure_e2e(h, api, a, b, args, flops, stream):
     vd = np.float64 if code == L.SPG_F64 else np.float32
     vsz = np.dtype(vd).itemsize
     h2d = sum(x[1].nbytes for x in ha + hb)
-    CT = 1 << 23            # C tiles per staged range
+    CT = max(1 << 16, args.e2e_range_tiles)  # C tiles per staged range
     VC = 1 << 27            # values per staged range (ranges halve when a range holds more)
     NW = max(1, args.e2e_copy_workers)
     NB = max(1, args.e2e_bands)
@@ -646,6 +646,8 @@ def main():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--e2e-bands", type=int, default=8,
                    help="tile-row bands of the e2e numeric phase (a band's values copy once it is complete)")
+    p.add_argument("--e2e-range-tiles", type=int, default=1 << 23,
+                   help="C tiles per staged e2e copy range (pinned staging per copy worker scales with it)")
     p.add_argument("--e2e-band-order", choices=["last", "first"], default="last",
                    help="e2e bands worked on from the last (light rows first, hub rows last) or the first")
     p.add_argument("--e2e-copy-workers", type=int, default=2,
