@@ -45,7 +45,7 @@ constexpr int NW_ARENA_F64 = 131072;  // one block per SM
 constexpr int NW_ARENA_MAX = 196608;
 template <typename ACC>
 constexpr int nw_arena() { return sizeof(ACC) == 4 ? NW_ARENA_F32 : NW_ARENA_F64; }
-constexpr int MAXA_SMEM = 512;  // A nonzeros per tile-row whose cursors fit in shared memory
+constexpr int MAXA_SMEM = 256;  // A nonzeros per tile-row whose cursors fit in shared memory
 constexpr int SWU = 4;          // 32-product steps per sweep round of a warp (loads in flight)
 
 __device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
