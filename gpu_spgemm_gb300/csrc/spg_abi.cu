@@ -380,20 +380,42 @@ extern "C" spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, con
 }
 
 // Step 3 on C tile-rows [r0, r1).
-static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
-                               spg_precision prec, spg_ctiles* C, int r0, int r1) {
+// The kernels step 3 runs on: row-wise windows, plain per-C-tile registers,
+// or plain with dense pairs on the tensor cores.
+enum class NumPath { ROWWISE, PLAIN, MIXED };
+
+// Checks that C is ready for step 3 (symbolic structure and masks) and picks
+// its path: MIXED for SPG_PREC_MIXED on FP32 data; ROWWISE when C's structure
+// came from the row-wise symbolic phase (or FP64 accumulation of FP32 data is
+// asked for); PLAIN otherwise.
+static spg_status numeric_path(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                               spg_precision prec, const spg_ctiles* C, NumPath* path) {
     SPG_TRY(validate_pair(h, A, B, C));
     if (!C->priv) return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic structure");
     if (C->numtileC > 0 && (!C->maskC || !C->tile_nnzC || !C->tile_valC))
         return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
-    if (r0 < 0 || r1 < r0 || r1 > C->tilem) return spg_fail(h, SPG_ERR_INVALID, "numeric: bad tile-row range");
-    CPriv* cp = static_cast<CPriv*>(C->priv);
+    const CPriv* cp = static_cast<const CPriv*>(C->priv);
     if (algo == SPG_ALGO_AUTO) algo = cp->algo;
     if (algo == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) algo = SPG_ALGO_PLAIN;
+    if (prec == SPG_PREC_MIXED && A->dtype == SPG_F32)
+        *path = NumPath::MIXED;
+    else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32))
+        *path = NumPath::ROWWISE;
+    else
+        *path = NumPath::PLAIN;
+    return SPG_OK;
+}
+
+static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
+                               spg_precision prec, spg_ctiles* C, int r0, int r1) {
+    NumPath path;
+    SPG_TRY(numeric_path(h, A, B, algo, prec, C, &path));
+    if (r0 < 0 || r1 < r0 || r1 > C->tilem) return spg_fail(h, SPG_ERR_INVALID, "numeric: bad tile-row range");
+    CPriv* cp = static_cast<CPriv*>(C->priv);
     const bool whole = r0 == 0 && r1 == C->tilem;
     SPG_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
-    const bool mixed = prec == SPG_PREC_MIXED && A->dtype == SPG_F32;
-    if (!mixed && (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32))) {
+    const bool mixed = path == NumPath::MIXED;
+    if (path == NumPath::ROWWISE) {
         SPG_TRY(rowwise_numeric(h, A, B, C, &cp->rw, prec, r0, r1));
     } else {
         int64_t t0 = 0, t1 = C->numtileC;  // C tiles of the tile-rows
@@ -439,15 +461,10 @@ extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, cons
         return spg_fail(h, SPG_ERR_INVALID, "numeric bands: bounds must run from 0 to tilem");
     for (int k = 0; k < nbands; k++)
         if (band_rows[k + 1] < band_rows[k]) return spg_fail(h, SPG_ERR_INVALID, "numeric bands: bounds descend");
-    if (!C->priv) return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic structure");
-    if (C->numtileC > 0 && (!C->maskC || !C->tile_nnzC || !C->tile_valC))
-        return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
+    NumPath path;
+    SPG_TRY(numeric_path(h, A, B, algo, prec, C, &path));
     CPriv* cp = static_cast<CPriv*>(C->priv);
-    spg_algo a = algo == SPG_ALGO_AUTO ? cp->algo : algo;
-    if (a == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) a = SPG_ALGO_PLAIN;
-    const bool mixed = prec == SPG_PREC_MIXED && A->dtype == SPG_F32;
-    const bool rowwise = !mixed && (a == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32));
-    if (!rowwise) {
+    if (path != NumPath::ROWWISE) {
         float ms = 0.f;
         for (int j = 0; j < nbands; j++) {
             const int k = last_first ? nbands - 1 - j : j;
