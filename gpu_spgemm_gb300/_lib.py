@@ -18,6 +18,7 @@ STATUS_NAMES = {0: "SPG_OK", 1: "SPG_ERR_INVALID", 2: "SPG_ERR_OOM", 3: "SPG_ERR
 SPG_F32, SPG_F64 = 0, 1
 SPG_LAYOUT_ROW, SPG_LAYOUT_B_CSC = 0, 1
 SPG_TILE_WITH_TILE_CSC = 1
+SPG_TILE = 16  # tile edge
 SPG_ALGO_AUTO, SPG_ALGO_PLAIN, SPG_ALGO_ROWWISE = 0, 1, 2
 SPG_PREC_F32, SPG_PREC_MIXED, SPG_PREC_F64 = 0, 1, 2
 SPG_BANDS_FIRST_TO_LAST, SPG_BANDS_LAST_TO_FIRST = 0, 1

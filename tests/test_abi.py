@@ -74,3 +74,18 @@ def _lib_load_fresh(path):
         return _lib.load(path)
     finally:
         _lib._lib = saved
+
+
+def test_enum_values_match_header():
+    """Every SPG_* constant the header defines (enums and #defines) has the
+    same value in the ctypes binding."""
+    from gpu_spgemm_gb300 import _lib as L
+    src = open(os.path.join(ROOT, "include", "spgemm_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    num = r"(-?(?:0[xX][0-9a-fA-F]+|\d+))"
+    found = {m.group(1): int(m.group(2), 0) for m in re.finditer(r"\b(SPG_[A-Z0-9_]+)\s*=\s*" + num, src)}
+    found.update({m.group(1): int(m.group(2), 0)
+                  for m in re.finditer(r"#define\s+(SPG_[A-Z0-9_]+)\s+\(?" + num, src)})
+    assert len(found) >= 20, found
+    for name, value in found.items():
+        assert getattr(L, name) == value, name
