@@ -47,7 +47,7 @@ class SpgCTiles(C.Structure):
 class SpgStats(C.Structure):
     _fields_ = [("ms_step1", C.c_float), ("ms_step2", C.c_float), ("ms_step3", C.c_float),
                 ("products", I64), ("overflow_reruns", I64), ("work_items", I64), ("tensor_pairs", I64),
-                ("fp64_tiles", I64), ("algo_used", I32), ("reserved", I32), ("predicted_tiles", I64)]
+                ("fp64_tiles", I64), ("algo_used", I32), ("sizing_fallbacks", I32), ("predicted_tiles", I64)]
 
 
 # spg_band_fn: (user, band, row_begin, row_end)
@@ -60,6 +60,7 @@ SIGNATURES = {
     "spg_set_stream": (I32, [P, P]),
     "spg_last_error": (C.c_char_p, [P]),
     "spg_get_stats": (I32, [P, C.POINTER(SpgStats)]),
+    "spg_kernel_launches": (I32, [P, C.POINTER(I64)]),
     "spg_tile_from_csr": (I32, [P, I32, I32, I64, P, P, P, I32, I32, I32, C.POINTER(SpgTiles)]),
     "spg_tile_from_csr_host": (I32, [P, I32, I32, I64, P, P, P, I32, I32, I32, C.POINTER(SpgTiles)]),
     "spg_tiles_free": (I32, [P, C.POINTER(SpgTiles)]),

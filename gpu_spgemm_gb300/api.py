@@ -68,6 +68,12 @@ class Handle:
         self.check(self.lib.spg_get_stats(self.h, C.byref(st)))
         return {k: getattr(st, k) for k, _ in L.SpgStats._fields_}
 
+    def launches(self) -> int:
+        """Kernels launched through this handle so far (a running count)."""
+        n = C.c_int64()
+        self.check(self.lib.spg_kernel_launches(self.h, C.byref(n)))
+        return n.value
+
     def close(self):
         if self.h:
             self.lib.spg_destroy(self.h)

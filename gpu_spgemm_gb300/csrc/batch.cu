@@ -153,12 +153,12 @@ static spg_status assemble(spg_handle_t h, spg_batch_t bt, const std::vector<int
         if (g > h->num_sms * 16) g = h->num_sms * 16;
         bd_rowptr_kernel<<<(int)g, 256, 0, h->stream>>>(rows, np, d_roff, d_mrows, d_nzoff, d_slot, rp_local, d_nnz,
                                                         rp_big);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
         if (NZ > 0) {
             int64_t g2 = ceil_div(NZ, 256);
             if (g2 > h->num_sms * 16) g2 = h->num_sms * 16;
             bd_colshift_kernel<<<(int)g2, 256, 0, h->stream>>>(NZ, np, d_nzoff, d_coff, ci_big);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
     }
     spg_status s = spg_tile_from_csr(h, (int)rows, (int)cols, NZ, rp_big, ci_big, val_big, bt->dtype,

@@ -120,24 +120,24 @@ extern "C" spg_status spg_csr_transpose(spg_handle_t h, int m, int n, int64_t nn
     if (m < 0 || n < 0 || nnz < 0 || nnz >= 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "transpose: bad size");
     if (!d_rp || !out_rp || (nnz > 0 && (!d_ci || !d_val || !out_ci || !out_val)))
         return spg_fail(h, SPG_ERR_INVALID, "transpose: null array");
+    ScratchList sc(h);
     int* hist = nullptr;
-    SPG_TRY(spg_alloc_t(h, &hist, (size_t)n + 1));
+    SPG_TRY(sc.alloc(&hist, (size_t)n + 1));
     SPG_CUDA(h, cudaMemsetAsync(hist, 0, sizeof(int) * ((size_t)n + 1), h->stream));
     if (nnz > 0) {
         col_hist_kernel<<<cgrid(h, nnz, 256), 256, 0, h->stream>>>(d_ci, nnz, hist);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i32(h, hist, out_rp, n));
-    spg_free_async(h, hist);
     if (nnz == 0) return SPG_OK;
     uint32_t *keys = nullptr, *perm = nullptr, *rows = nullptr;
-    SPG_TRY(spg_alloc_t(h, &keys, (size_t)nnz));
-    SPG_TRY(spg_alloc_t(h, &perm, (size_t)nnz));
-    SPG_TRY(spg_alloc_t(h, &rows, (size_t)nnz));
+    SPG_TRY(sc.alloc(&keys, (size_t)nnz));
+    SPG_TRY(sc.alloc(&perm, (size_t)nnz));
+    SPG_TRY(sc.alloc(&rows, (size_t)nnz));
     copy_u32_kernel<<<cgrid(h, nnz, 256), 256, 0, h->stream>>>(d_ci, keys, nnz);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     row_ids_kernel<<<cgrid(h, (int64_t)m * 32, 256), 256, 0, h->stream>>>(m, d_rp, rows);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     // the original position of each entry: its index (entries are in row order)
     SPG_TRY(spg_iota_u32(h, perm, nnz));
     int bits = 1;
@@ -149,38 +149,32 @@ extern "C" spg_status spg_csr_transpose(spg_handle_t h, int m, int n, int64_t nn
     else
         transpose_gather_kernel<float><<<cgrid(h, nnz, 256), 256, 0, h->stream>>>(
             nnz, perm, rows, (const float*)d_val, out_ci, (float*)out_val);
-    SPG_CUDA(h, cudaGetLastError());
-    spg_free_async(h, keys);
-    spg_free_async(h, perm);
-    spg_free_async(h, rows);
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
 spg_status ctiles_to_csr_impl(spg_handle_t h, const spg_ctiles* C, int* out_rp, int* out_ci, void* out_val,
                               int64_t* nnz_out) {
     const int m = C->m;
+    ScratchList sc(h);
     int* cnt = nullptr;
     int64_t* rp64 = nullptr;
-    SPG_TRY(spg_alloc_t(h, &cnt, (size_t)m + 1));
-    SPG_TRY(spg_alloc_t(h, &rp64, (size_t)m + 1));
+    SPG_TRY(sc.alloc(&cnt, (size_t)m + 1));
+    SPG_TRY(sc.alloc(&rp64, (size_t)m + 1));
     SPG_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t)m + 1), h->stream));
     if (C->numtileC > 0) {
         ctile_rowcount_kernel<<<cgrid(h, C->numtileC * TS, 256), 256, 0, h->stream>>>(C->numtileC, m, C->tile_rowidxC,
                                                                                       C->maskC, cnt);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, rp64, m));
     int64_t nnz = 0;
     SPG_TRY(spg_read_i64(h, rp64 + m, &nnz));
     if (nnz_out) *nnz_out = nnz;
-    if (!out_rp) {
-        spg_free_async(h, cnt);
-        spg_free_async(h, rp64);
-        return SPG_OK;
-    }
+    if (!out_rp) return SPG_OK;
     if (nnz >= 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "to_csr: nnz does not fit int32 CSR");
     i64_to_i32_rp_kernel<<<cgrid(h, m + 1, 256), 256, 0, h->stream>>>(rp64, out_rp, m + 1);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     if (nnz > 0 && C->tilem > 0) {
         if (C->dtype == SPG_F64)
             ctile_fill_kernel<double><<<cgrid(h, (int64_t)C->tilem * 32, 256), 256, 0, h->stream>>>(
@@ -190,10 +184,8 @@ spg_status ctiles_to_csr_impl(spg_handle_t h, const spg_ctiles* C, int* out_rp, 
             ctile_fill_kernel<float><<<cgrid(h, (int64_t)C->tilem * 32, 256), 256, 0, h->stream>>>(
                 C->tilem, m, C->tile_ptrC, C->tile_colidxC, C->maskC, C->tile_nnzC, C->ptrRowC,
                 (const float*)C->tile_valC, rp64, out_ci, (float*)out_val);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
-    spg_free_async(h, cnt);
-    spg_free_async(h, rp64);
     return SPG_OK;
 }
 
@@ -232,6 +224,7 @@ extern "C" spg_status spg_galerkin(spg_handle_t h, int m, int nc, int64_t nnzA, 
     GTRY(spg_tile_from_csr(h, m, nc, nnzP, P_rp, P_ci, P_val, dtype, SPG_LAYOUT_B_CSC, 0, &tP));
     GTRY(spg_products(h, &tA, &tP, &prod1));
     GTRY(spg_spgemm(h, &tA, &tP, algo, prec, &AP));
+    const spg_stats first = h->stats;
     GTRY(ctiles_to_csr_impl(h, &AP, nullptr, nullptr, nullptr, &nnzAP));
     GTRY(spg_alloc_t(h, &ap_rp, (size_t)m + 1));
     GTRY(spg_alloc_t(h, &ap_ci, (size_t)nnzAP + 1));
@@ -247,6 +240,18 @@ extern "C" spg_status spg_galerkin(spg_handle_t h, int m, int nc, int64_t nnzA, 
     GTRY(spg_products(h, &tPT, &tAP, &prod2));
     GTRY(spg_spgemm(h, &tPT, &tAP, algo, prec, RAP));
 #undef GTRY
+    // the call's statistics cover both products
+    spg_stats& st = h->stats;
+    st.ms_step1 += first.ms_step1;
+    st.ms_step2 += first.ms_step2;
+    st.ms_step3 += first.ms_step3;
+    st.products += first.products;
+    st.overflow_reruns += first.overflow_reruns;
+    st.work_items += first.work_items;
+    st.tensor_pairs += first.tensor_pairs;
+    st.fp64_tiles += first.fp64_tiles;
+    st.sizing_fallbacks += first.sizing_fallbacks;
+    st.predicted_tiles += first.predicted_tiles;
     if (products_out) *products_out = prod1 + prod2;
     cleanup();
     return SPG_OK;

@@ -226,13 +226,21 @@ __global__ void mlp_adam_kernel(float* __restrict__ p, float* __restrict__ g, fl
     g[t] = 0.f;
 }
 
-// predicted counts -> per-tile-row capacity, summed
 // Slot size of each tile-row: the predicted C tile count (the network's
-// target is log1p of it) grown by the margin, plus 2.
-__global__ void mlp_slot_kernel(int tilem, const float* __restrict__ pred, float margin, int* __restrict__ slot) {
+// target is log1p of it) grown by the margin, plus 2, and never more than the
+// row can have: no more than B's tile columns, than the tile pairs the row
+// reaches (feature 2) or than the span of tile columns they cover (feature 5).
+// Those bounds come back from log1p-encoded floats, so they get 1e-4 of
+// relative slack and 2 tiles on top (a bound read low only sends the row to
+// the exact re-fill).  A wild prediction therefore never asks for more
+// staging than an exact upper-bound pass would.
+__global__ void mlp_slot_kernel(int tilem, int tilenB, const float* __restrict__ feat,
+                                const float* __restrict__ pred, float margin, int* __restrict__ slot) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
         const float t = fmaxf(expm1f(fmaxf(pred[(int64_t)i * NO + 0], 0.f)), 0.f);
-        slot[i] = (int)fminf(ceilf(t * (1.f + margin) + 2.f), 1.0e9f);
+        const float* f = feat + (int64_t)i * NF;
+        const float bound = fminf(fminf(expm1f(f[2]), expm1f(f[5])) * 1.0001f + 2.f, (float)tilenB);
+        slot[i] = (int)fminf(ceilf(t * (1.f + margin) + 2.f), fmaxf(ceilf(bound), 0.f));
     }
 }
 
@@ -318,7 +326,7 @@ extern "C" spg_status spg_mlp_features(spg_handle_t h, const spg_tiles* A, const
     mlp_features_kernel<<<mgrid(h, (int64_t)A->tilem * 32, 256), 256, 0, h->stream>>>(
         A->tilem, A->m, B->tilen, A->tile_ptr, A->tile_columnidx, A->row_ptr, A->col_idx, B->tile_ptr,
         B->tile_columnidx, B->row_ptr, d_feat);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -326,7 +334,7 @@ extern "C" spg_status spg_mlp_forward(spg_handle_t h, spg_mlp_t mm, const float*
     if (!h || !mm) return SPG_ERR_INVALID;
     if (n <= 0) return SPG_OK;
     mlp_forward_kernel<<<mgrid(h, n, 128), 128, 0, h->stream>>>(n, mm->d_param, mm->d_norm, d_feat, d_out);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -339,7 +347,7 @@ extern "C" spg_status spg_mlp_gradient(spg_handle_t h, spg_mlp_t mm, const float
     SPG_CUDA(h, cudaMemsetAsync(mm->d_loss, 0, 4, h->stream));
     mlp_grad_kernel<<<mgrid(h, n, 128), 128, 0, h->stream>>>(n, nullptr, mm->d_param, mm->d_norm, d_feat, d_target,
                                                             d_grad_out, mm->d_loss);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     if (loss_out) {
         SPG_CUDA(h, cudaMemcpyAsync(loss_out, mm->d_loss, 4, cudaMemcpyDeviceToHost, h->stream));
         SPG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -365,12 +373,12 @@ extern "C" spg_status spg_mlp_train(spg_handle_t h, spg_mlp_t mm, const float* d
                                                                      perm ? d_feat : d_feat + s0 * NF,
                                                                      perm ? d_target : d_target + s0 * NO,
                                                                      mm->d_grad, mm->d_loss);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
             mm->step++;
             const float c1 = 1.f - std::pow(b1, (float)mm->step), c2 = 1.f - std::pow(b2, (float)mm->step);
             mlp_adam_kernel<<<(NPARAM + 255) / 256, 256, 0, h->stream>>>(mm->d_param, mm->d_grad, mm->d_m, mm->d_v,
                                                                           lr, b1, b2, c1, c2);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
             nbatch++;
         }
         if (last_epoch_loss && ep == epochs - 1) {
@@ -394,16 +402,16 @@ extern "C" spg_status spg_set_sizing_model(spg_handle_t h, spg_mlp_t mm, float m
 spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz) {
     spg_mlp_t mm = h->sizing;
     const int tilem = A->tilem;
+    ScratchList sc(h);
     float *feat = nullptr, *pred = nullptr;
-    SPG_TRY(spg_alloc_t(h, &feat, (size_t)tilem * NF + 1));
-    SPG_TRY(spg_alloc_t(h, &pred, (size_t)tilem * NO + 1));
+    SPG_TRY(sc.alloc(&feat, (size_t)tilem * NF + 1));
+    SPG_TRY(sc.alloc(&pred, (size_t)tilem * NO + 1));
     SPG_TRY(spg_mlp_features(h, A, B, feat));
     SPG_TRY(spg_mlp_forward(h, mm, feat, tilem, pred));
     if (tilem > 0) {
-        mlp_slot_kernel<<<mgrid(h, tilem, 256), 256, 0, h->stream>>>(tilem, pred, h->sizing_margin, slot_sz);
-        SPG_CUDA(h, cudaGetLastError());
+        mlp_slot_kernel<<<mgrid(h, tilem, 256), 256, 0, h->stream>>>(tilem, B->tilen, feat, pred, h->sizing_margin,
+                                                                   slot_sz);
+        SPG_LAUNCHED(h);
     }
-    spg_free_async(h, feat);
-    spg_free_async(h, pred);
     return SPG_OK;
 }

@@ -200,17 +200,17 @@ extern "C" spg_status spg_ctiles_to_csr_noalloc(spg_handle_t h, const spg_ctiles
     if (C->numtileC > 0) {
         na_rowcount_kernel<<<na_grid(h, C->numtileC * TS, 256), 256, 0, h->stream>>>(C->numtileC, m, C->tile_rowidxC,
                                                                                     C->maskC, sc->counts);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     if (nb > 0) {
         na_block_sum_kernel<<<nb, 256, 0, h->stream>>>(m, sc->counts, sc->block_sums);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     na_block_scan_kernel<<<1, 1024, 0, h->stream>>>(nb, sc->block_sums);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     if (nb > 0) {
         na_rowptr_kernel<<<nb, 256, 0, h->stream>>>(m, sc->counts, sc->block_sums, nb, out_rp);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     } else {
         SPG_CUDA(h, cudaMemsetAsync(out_rp, 0, sizeof(int), h->stream));
     }
@@ -223,7 +223,7 @@ extern "C" spg_status spg_ctiles_to_csr_noalloc(spg_handle_t h, const spg_ctiles
             na_fill_kernel<float><<<na_grid(h, (int64_t)C->tilem * 32, 256), 256, 0, h->stream>>>(
                 C->tilem, m, C->tile_ptrC, C->tile_colidxC, C->maskC, C->tile_nnzC, C->ptrRowC,
                 (const float*)C->tile_valC, out_rp, out_ci, (float*)out_val);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     if (nnz) *nnz = C->nnzC;
     return SPG_OK;

@@ -6,6 +6,8 @@
 // the row-wise binned path is measured against.
 #include <cuda_fp16.h>
 
+#include <cstdlib>
+
 #include "spg_common.cuh"
 #include "plain.cuh"
 
@@ -693,15 +695,16 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
         return spg_fail(h, SPG_ERR_UNSUPPORTED, "step 1: B has too many tile columns for one bitmap");
     SPG_CUDA(h, cudaFuncSetAttribute(c1_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SPG_CUDA(h, cudaFuncSetAttribute(c1_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ScratchList sc(h);
     int* cnt = nullptr;
     int64_t* ptr64 = nullptr;
-    SPG_TRY(spg_alloc_t(h, &cnt, (size_t)tilem + 1));
-    SPG_TRY(spg_alloc_t(h, &ptr64, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&ptr64, (size_t)tilem + 1));
     if (tilem > 0) {
         c1_count_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx,
                                                                B->tile_ptr, B->tile_columnidx, cnt, row_pairs,
                                                                pairs_total);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
     int64_t numtileC = 0;
@@ -710,17 +713,15 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     C->numtileC = numtileC;
     SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
     i64_to_i32_kernel<<<grid_cap(h, tilem + 1, 256, 8), 256, 0, h->stream>>>(ptr64, C->tile_ptrC, tilem + 1);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     SPG_TRY(spg_alloc_t(h, &C->tile_rowidxC, (size_t)numtileC + 1));
     SPG_TRY(spg_alloc_t(h, &C->tile_colidxC, (size_t)numtileC + 1));
     if (tilem > 0 && numtileC > 0) {
         c1_fill_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                               B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
                                                               C->tile_colidxC, nullptr);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
-    spg_free_async(h, cnt);
-    spg_free_async(h, ptr64);
     return SPG_OK;
 }
 
@@ -738,23 +739,33 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
         return spg_fail(h, SPG_ERR_UNSUPPORTED, "step 1: B has too many tile columns for one bitmap");
     SPG_CUDA(h, cudaFuncSetAttribute(c1_slot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SPG_CUDA(h, cudaFuncSetAttribute(c1_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ScratchList sc(h);
     int64_t* slot_off = nullptr;
-    SPG_TRY(spg_alloc_t(h, &slot_off, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&slot_off, (size_t)tilem + 1));
     SPG_TRY(spg_scan_i32_to_i64(h, slot_sz, slot_off, tilem));
     int64_t cap = 0;
     SPG_TRY(spg_read_i64(h, slot_off + tilem, &cap));
     h->stats.predicted_tiles = cap;
+    {   // the staging may take a quarter of the free device memory (C's arrays
+        // come after it); beyond that the caller runs the exact two passes
+        size_t fr = 0, tot = 0;
+        SPG_CUDA(h, cudaMemGetInfo(&fr, &tot));
+        unsigned long long budget = fr / 4;
+        if (const char* e = getenv("SPG_SLOT_BUDGET_BYTES")) budget = strtoull(e, nullptr, 10);
+        if ((unsigned long long)cap * sizeof(int) > budget)
+            return spg_fail(h, SPG_ERR_OOM, "step 1: predicted slots exceed the staging budget");
+    }
     int* slot_col = nullptr;
     int* cnt = nullptr;
     int64_t* ptr64 = nullptr;
-    SPG_TRY(spg_alloc_t(h, &slot_col, (size_t)cap + 1));
-    SPG_TRY(spg_alloc_t(h, &cnt, (size_t)tilem + 1));
-    SPG_TRY(spg_alloc_t(h, &ptr64, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&slot_col, (size_t)cap + 1));
+    SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&ptr64, (size_t)tilem + 1));
     if (tilem > 0) {
         c1_slot_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                               B->tile_columnidx, slot_off, slot_col, cnt, row_pairs,
                                                               pairs_total);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
     int64_t numtileC = 0;
@@ -763,7 +774,7 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
     C->numtileC = numtileC;
     SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
     i64_to_i32_kernel<<<grid_cap(h, tilem + 1, 256, 8), 256, 0, h->stream>>>(ptr64, C->tile_ptrC, tilem + 1);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     SPG_TRY(spg_alloc_t(h, &C->tile_rowidxC, (size_t)numtileC + 1));
     SPG_TRY(spg_alloc_t(h, &C->tile_colidxC, (size_t)numtileC + 1));
     int* over_rows = cnt;  // reused: counts are no longer needed
@@ -772,7 +783,7 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
     if (tilem > 0 && numtileC > 0) {
         c1_compact_kernel<<<grid_cap(h, (int64_t)tilem * 32, 256, 16), 256, 0, h->stream>>>(
             tilem, C->tile_ptrC, slot_off, slot_col, C->tile_rowidxC, C->tile_colidxC, over_rows, n_over);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
         int nov = 0;
         SPG_TRY(spg_read_i32(h, reinterpret_cast<const int*>(n_over), &nov));
         if (nov > 0) {  // prediction too small for these rows: exact fill of just them
@@ -780,13 +791,9 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
             c1_fill_kernel<<<nov, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                                 B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
                                                                 C->tile_colidxC, over_rows);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
     }
-    spg_free_async(h, slot_off);
-    spg_free_async(h, slot_col);
-    spg_free_async(h, cnt);
-    spg_free_async(h, ptr64);
     return SPG_OK;
 }
 
@@ -809,7 +816,7 @@ spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
                 A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, tile_cnt,
                 nullptr, nullptr, nullptr, nullptr, 0, ctr, ctr + 1, h->d_flags);
         }
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
         if (pp->spec_cap == 0) break;
         // overflow re-run (src/spgemm_raw_v2.cu:191-200, with the bound honoured in-kernel)
         int64_t used = 0;
@@ -876,7 +883,7 @@ static spg_status plain_step3_t(spg_handle_t h, const spg_tiles* A, const spg_ti
             (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
             B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,
             (V*)C->tile_valC, C->tile_colC, nullptr, nullptr, nullptr, nullptr);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -909,7 +916,7 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
         SPG_TRY(spg_alloc_t(h, slot, (size_t)n + 1));
         if (n > 0) {
             dense_flag_kernel<<<grid_cap(h, n, 256, 8), 256, 0, h->stream>>>(n, T->tile_nnz, dense_thr, *slot);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
         SPG_TRY(spg_scan_i32_to_i32(h, *slot, *slot, n));
         int nd = 0;
@@ -922,7 +929,7 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
             else
                 dense_frag_kernel<false><<<grid_cap(h, n * 32, 256, 16), 256, 0, h->stream>>>(
                     n, T->tile_nnz, (const float*)T->tile_csr_Val, T->tile_csr_Ptr, T->mask, dense_thr, *slot, *frag);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
         return SPG_OK;
     };
@@ -947,7 +954,7 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
         c3_numeric_kernel<float, false, true><<<grid, 256, 0, h->stream>>>(REG_ARGS, nullptr, nullptr, nullptr, nullptr,
                                                                            dense_thr, dense_tiles, n_dense);
 #undef REG_ARGS
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     int nd_tiles = 0;
     SPG_TRY(spg_read_i32(h, reinterpret_cast<const int*>(n_dense), &nd_tiles));
     // 2. the listed tiles' dense pairs on tensor cores, added to their values
@@ -969,7 +976,7 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
 #undef TENSOR_ARGS
     }
     spg_free_async(h, dense_tiles);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     int64_t v[2] = {0, 0};
     SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 20, ctr, 16, cudaMemcpyDeviceToHost, h->stream));
     SPG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -984,7 +991,7 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
             (const float*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
             B->tile_nnz, (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask,
             cv.ptr16, (float*)C->tile_valC);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     spg_free_async(h, ctr);
     spg_free_async(h, list);

@@ -695,10 +695,11 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
                              RowwisePriv* rp) {
     if (rp->item_prefix) return SPG_OK;
     const int tilem = C->tilem;
+    ScratchList sc(h);
     int64_t* nit = nullptr;
     int64_t* prod = nullptr;
-    SPG_TRY(spg_alloc_t(h, &nit, (size_t)tilem + 1));
-    SPG_TRY(spg_alloc_t(h, &prod, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&nit, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&prod, (size_t)tilem + 1));
     SPG_TRY(spg_alloc_t(h, &rp->item_prefix, (size_t)tilem + 1));
     SPG_TRY(spg_alloc_t(h, &rp->counters, 4));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters, 0, 4 * sizeof(unsigned long long), h->stream));
@@ -707,15 +708,13 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
         if (g > h->num_sms * 8) g = h->num_sms * 8;
         rw_plan_kernel<<<g, 256, 0, h->stream>>>(tilem, A->m, C->tile_ptrC, A->row_ptr, A->col_idx, B->row_ptr, prod,
                                                  rp->counters + 2, rp->counters + 3);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
         int g2 = (int)ceil_div(tilem, 256);
         if (g2 > h->num_sms * 8) g2 = h->num_sms * 8;
         rw_plan2_kernel<<<g2, 256, 0, h->stream>>>(tilem, h->num_sms, C->tile_ptrC, prod, rp->counters + 3, nit);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i64_to_i64(h, nit, rp->item_prefix, tilem));
-    spg_free_async(h, nit);
-    spg_free_async(h, prod);
     SPG_TRY(spg_read_i64(h, rp->item_prefix + tilem, &rp->nitems));
     int64_t mx = 0;
     SPG_TRY(spg_read_i64(h, (const int64_t*)(rp->counters + 2), &mx));
@@ -746,7 +745,7 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     rw_symbolic_kernel<<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, A->row_ptr,
         A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -803,7 +802,7 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
         C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
         (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na,
         ba.nbands, ba.band_end, ba.band_cnt, ba.band_flag, ba.rev, arena);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -831,7 +830,7 @@ spg_status rowwise_numeric_bands_launch(spg_handle_t h, const spg_tiles* A, cons
     SPG_TRY(rw_prepare(h, A, B, C, rp));
     band_plan_kernel<<<(nbands + 255) / 256, 256, 0, h->stream>>>(nbands, d_rows, rp->item_prefix, d_band_end,
                                                                   d_band_cnt);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     SPG_CUDA(h, cudaMemcpyAsync(h_band_end, d_band_end, (size_t)nbands * sizeof(int64_t), cudaMemcpyDeviceToHost,
                                 h->stream));
     SPG_CUDA(h, cudaStreamSynchronize(h->stream));

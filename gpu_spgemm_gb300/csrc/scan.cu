@@ -146,14 +146,14 @@ spg_status scan_long(spg_handle_t h, const Tin* in, Tout* out, int64_t n) {
     const int64_t nslices = ceil_div(n + 1, WS_SLICE);
     const int64_t nblocks = ceil_div(nslices, WS_THREADS / 32);
     if (nblocks > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "scan: too long");
+    ScratchList sc(h);
     int64_t* sums = nullptr;
-    SPG_TRY(spg_alloc_t(h, &sums, (size_t)nslices + 1));
+    SPG_TRY(sc.alloc(&sums, (size_t)nslices + 1));
     slice_sum_kernel<Tin><<<(unsigned)nblocks, WS_THREADS, 0, h->stream>>>(in, n, nslices, sums);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     SPG_TRY((scan_impl<int64_t, int64_t>(h, sums, sums, nslices)));
     slice_scan_kernel<Tin, Tout><<<(unsigned)nblocks, WS_THREADS, 0, h->stream>>>(in, out, n, nslices, sums);
-    SPG_CUDA(h, cudaGetLastError());
-    spg_free_async(h, sums);
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -163,14 +163,14 @@ spg_status scan_impl(spg_handle_t h, const Tin* in, Tout* out, int64_t n) {
     if (n >= WS_MIN_N) return scan_long<Tin, Tout>(h, in, out, n);
     const int64_t nblocks = ceil_div(n + 1, SCAN_TILE);
     if (nblocks > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "scan: too long");
+    ScratchList sc(h);
     unsigned long long* state = nullptr;
-    SPG_TRY(spg_alloc(h, (void**)&state, sizeof(unsigned long long) * nblocks + 16));
+    SPG_TRY(sc.alloc(&state, (size_t)nblocks + 2));
     unsigned* ticket = reinterpret_cast<unsigned*>(state + nblocks);
     SPG_CUDA(h, cudaMemsetAsync(state, 0, sizeof(unsigned long long) * nblocks + 16, h->stream));
     scan_lookback_kernel<Tin, Tout><<<(unsigned)nblocks, SCAN_THREADS, 0, h->stream>>>(
         in, out, n, state, ticket, h->d_flags);
-    SPG_CUDA(h, cudaGetLastError());
-    spg_free_async(h, state);
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -252,7 +252,7 @@ spg_status spg_iota_u32(spg_handle_t h, uint32_t* v, int64_t n) {
     int64_t g = ceil_div(n, 256);
     if (g > (int64_t)h->num_sms * 16) g = (int64_t)h->num_sms * 16;
     iota_u32_kernel<<<(int)g, 256, 0, h->stream>>>(v, n);
-    SPG_CUDA(h, cudaGetLastError());
+    SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
@@ -274,16 +274,17 @@ spg_status spg_radix_sort_pairs(spg_handle_t h, uint32_t* keys, uint32_t* vals, 
     const int nblk = (int)ceil_div(n, RS_CHUNK);
     uint32_t *k2 = nullptr, *v2 = nullptr;
     int* hist = nullptr;
-    SPG_TRY(spg_alloc_t(h, &k2, n));
-    SPG_TRY(spg_alloc_t(h, &v2, n));
-    SPG_TRY(spg_alloc_t(h, &hist, (int64_t)256 * nblk + 1));
+    ScratchList sc(h);
+    SPG_TRY(sc.alloc(&k2, n));
+    SPG_TRY(sc.alloc(&v2, n));
+    SPG_TRY(sc.alloc(&hist, (int64_t)256 * nblk + 1));
     uint32_t *ka = keys, *va = vals, *kb = k2, *vb = v2;
     for (int p = 0; p < passes; p++) {
         radix_hist_kernel<<<nblk, RS_THREADS, 0, h->stream>>>(ka, n, 8 * p, nblk, hist);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
         SPG_TRY(spg_scan_i32_to_i32(h, hist, hist, (int64_t)256 * nblk));
         radix_scatter_kernel<<<nblk, RS_THREADS, 0, h->stream>>>(ka, va, kb, vb, n, 8 * p, nblk, hist);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
         uint32_t* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
     }
@@ -291,8 +292,5 @@ spg_status spg_radix_sort_pairs(spg_handle_t h, uint32_t* keys, uint32_t* vals, 
         SPG_CUDA(h, cudaMemcpyAsync(keys, ka, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
         SPG_CUDA(h, cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     }
-    spg_free_async(h, k2);
-    spg_free_async(h, v2);
-    spg_free_async(h, hist);
     return SPG_OK;
 }

@@ -151,6 +151,12 @@ extern "C" spg_status spg_get_stats(spg_handle_t h, spg_stats* out) {
     return SPG_OK;
 }
 
+extern "C" spg_status spg_kernel_launches(spg_handle_t h, int64_t* out) {
+    if (!h || !out) return SPG_ERR_INVALID;
+    *out = h->launches;
+    return SPG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // tiling
 // ---------------------------------------------------------------------------
@@ -266,12 +272,30 @@ static spg_status tiles_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
     SPG_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
     // ---- step 1: C tile structure
     if (h->sizing) {
-        int* slot = nullptr;
-        SPG_TRY(spg_alloc_t(h, &slot, (size_t)A->tilem + 1));
-        SPG_TRY(mlp_predict_rows(h, A, B, slot));
-        const spg_status st = plain_step1_sized(h, A, B, C, cp->row_pairs, cp->plain.counters + 2, slot);
-        spg_free_async(h, slot);
-        SPG_TRY(st);
+        spg_status st;
+        {
+            ScratchList sc(h);
+            int* slot = nullptr;
+            st = sc.alloc(&slot, (size_t)A->tilem + 1);
+            if (st == SPG_OK) st = mlp_predict_rows(h, A, B, slot);
+            if (st == SPG_OK) st = plain_step1_sized(h, A, B, C, cp->row_pairs, cp->plain.counters + 2, slot);
+        }
+        if (st == SPG_ERR_OOM) {
+            // The predicted slots (or C's arrays beside them) did not fit:
+            // drop what the sized pass allocated and run the exact two-pass
+            // step 1, which needs no staging.  The structure is the same.
+            spg_free_async(h, C->tile_ptrC);
+            spg_free_async(h, C->tile_rowidxC);
+            spg_free_async(h, C->tile_colidxC);
+            C->tile_ptrC = C->tile_rowidxC = C->tile_colidxC = nullptr;
+            C->numtileC = 0;
+            h->stats.overflow_reruns = 0;
+            h->stats.sizing_fallbacks++;
+            SPG_CUDA(h, cudaMemsetAsync(cp->plain.counters + 2, 0, sizeof(unsigned long long), h->stream));
+            SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
+        } else {
+            SPG_TRY(st);
+        }
     } else {
         SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
     }
@@ -671,7 +695,7 @@ extern "C" spg_status spg_products(spg_handle_t h, const spg_tiles* A, const spg
         int64_t g = ceil_div(A->nnz, 256);
         if (g > h->num_sms * 8) g = h->num_sms * 8;
         products_kernel<<<(int)g, 256, 0, h->stream>>>(A->nnz, A->col_idx, B->row_ptr, d);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_read_i64(h, (const int64_t*)d, out));
     spg_free_async(h, d);

@@ -88,6 +88,7 @@ struct spg_handle_s {
     int num_sms = 0;
     size_t smem_optin = 0;
     size_t smem_per_sm = 0;
+    int64_t launches = 0;             // kernels launched through this handle
 };
 
 spg_status spg_fail(spg_handle_t h, spg_status s, const std::string& msg);
@@ -97,6 +98,14 @@ spg_status spg_cuda_fail(spg_handle_t h, cudaError_t e, const char* what);
     do {                                                               \
         cudaError_t _e = (call);                                       \
         if (_e != cudaSuccess) return spg_cuda_fail((h), _e, #call);   \
+    } while (0)
+
+// After a kernel launch: counts the launch on the handle (spg_kernel_launches)
+// and turns a launch error into a status.
+#define SPG_LAUNCHED(h)                                                \
+    do {                                                               \
+        (h)->launches++;                                               \
+        SPG_CUDA((h), cudaGetLastError());                             \
     } while (0)
 
 #define SPG_TRY(call)                          \
@@ -112,6 +121,38 @@ template <typename T>
 inline spg_status spg_alloc_t(spg_handle_t h, T** p, size_t count) {
     return spg_alloc(h, reinterpret_cast<void**>(p), count * sizeof(T));
 }
+
+// Device scratch of one call: every buffer taken through it is released
+// (stream-ordered, after the work queued so far) when the scope ends, on
+// every return path, so an error return leaks nothing.
+class ScratchList {
+  public:
+    explicit ScratchList(spg_handle_t h) : h_(h) {}
+    ScratchList(const ScratchList&) = delete;
+    ScratchList& operator=(const ScratchList&) = delete;
+    ~ScratchList() {
+        for (int i = 0; i < n_; i++) spg_free_async(h_, p_[i]);
+    }
+    template <typename T>
+    spg_status alloc(T** out, size_t count) {
+        *out = nullptr;
+        if (n_ == kMax) return spg_fail(h_, SPG_ERR_INVALID, "internal: too many scratch buffers in one call");
+        SPG_TRY(spg_alloc_t(h_, out, count));
+        p_[n_++] = *out;
+        return SPG_OK;
+    }
+    // Hands a buffer over to a longer-lived owner: it is no longer released.
+    void keep(const void* p) {
+        for (int i = 0; i < n_; i++)
+            if (p_[i] == p) p_[i] = nullptr;
+    }
+
+  private:
+    static constexpr int kMax = 16;
+    spg_handle_t h_;
+    void* p_[kMax] = {};
+    int n_ = 0;
+};
 
 // Read device error bits (synchronises the stream) and clear them.
 spg_status spg_check_flags(spg_handle_t h, const char* where);

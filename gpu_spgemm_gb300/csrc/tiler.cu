@@ -349,8 +349,9 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
     const int* ci = out->col_idx;
 
     // pass 1: tiles per tile-row
+    ScratchList sc(h);
     int* tile_cnt_rows = nullptr;
-    SPG_TRY(spg_alloc_t(h, &tile_cnt_rows, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&tile_cnt_rows, (size_t)tilem + 1));
     SPG_TRY(spg_alloc_t(h, &out->tile_ptr, (size_t)tilem + 1));
     const size_t smem1 = sizeof(uint32_t) * nwords;
     const size_t smem2 = 2 * sizeof(uint32_t) * nwords;
@@ -358,14 +359,13 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
     SPG_CUDA(h, cudaFuncSetAttribute(tiler_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
     if (tilem > 0) {
         tiler_count_kernel<<<tilem, TL_THREADS, smem1, h->stream>>>(m, n, nwords, rp, ci, tile_cnt_rows, h->d_flags);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i32(h, tile_cnt_rows, out->tile_ptr, tilem));
     int numtile = 0;
     SPG_TRY(spg_read_i32(h, out->tile_ptr + tilem, &numtile));
     SPG_TRY(spg_check_flags(h, "tiling"));
     out->numtile = numtile;
-    spg_free_async(h, tile_cnt_rows);
 
     // pass 2: tile columns, segment counts and masks
     int* tile_rowof = nullptr;
@@ -375,23 +375,23 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
     uint16_t* mask_row = nullptr;
     int* cnt_row = nullptr;
     SPG_TRY(spg_alloc_t(h, &out->tile_columnidx, (size_t)numtile + 1));
-    SPG_TRY(spg_alloc_t(h, &tile_rowof, (size_t)numtile + 1));
-    SPG_TRY(spg_alloc_t(h, &tmp_t, (size_t)nnz + 1));
-    SPG_TRY(spg_alloc_t(h, &tmp_rp, (size_t)nnz + 1));
-    SPG_TRY(spg_alloc_t(h, &ptr_row, (size_t)numtile * TS + 16));
-    SPG_TRY(spg_alloc_t(h, &mask_row, (size_t)numtile * TS + 16));
-    SPG_TRY(spg_alloc_t(h, &cnt_row, (size_t)numtile + 1));
+    SPG_TRY(sc.alloc(&tile_rowof, (size_t)numtile + 1));
+    SPG_TRY(sc.alloc(&tmp_t, (size_t)nnz + 1));
+    SPG_TRY(sc.alloc(&tmp_rp, (size_t)nnz + 1));
+    SPG_TRY(sc.alloc(&ptr_row, (size_t)numtile * TS + 16));
+    SPG_TRY(sc.alloc(&mask_row, (size_t)numtile * TS + 16));
+    SPG_TRY(sc.alloc(&cnt_row, (size_t)numtile + 1));
     SPG_CUDA(h, cudaMemsetAsync(ptr_row, 0, (size_t)numtile * TS, h->stream));
     SPG_CUDA(h, cudaMemsetAsync(mask_row, 0, sizeof(uint16_t) * (size_t)numtile * TS, h->stream));
     if (tilem > 0) {
         tiler_fill_kernel<<<tilem, TL_THREADS, smem2, h->stream>>>(m, nwords, rp, ci, out->tile_ptr,
                                                                    out->tile_columnidx, tile_rowof, ptr_row,
                                                                    mask_row, tmp_t, tmp_rp);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     if (numtile > 0) {
         tile_rowscan_kernel<<<(unsigned)ceil_div(numtile, 256), 256, 0, h->stream>>>(numtile, ptr_row, cnt_row);
-        SPG_CUDA(h, cudaGetLastError());
+        SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_alloc_t(h, &out->tile_nnz, (size_t)numtile + 1));
     SPG_TRY(spg_alloc(h, &out->tile_csr_Val, vs * ((size_t)nnz + 1)));
@@ -399,10 +399,10 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
 
     if (layout == SPG_LAYOUT_ROW) {
         SPG_TRY(spg_scan_i32_to_i32(h, cnt_row, out->tile_nnz, numtile));
-        out->tile_csr_Ptr = ptr_row;
+        out->tile_csr_Ptr = ptr_row;  // the row-major per-tile arrays are the result
         out->mask = mask_row;
-        ptr_row = nullptr;
-        mask_row = nullptr;
+        sc.keep(ptr_row);
+        sc.keep(mask_row);
         if (nnz > 0) {
             if (dtype == SPG_F64)
                 tiler_scatter_kernel<double><<<grid_for(h, nnz, 256), 256, 0, h->stream>>>(
@@ -412,17 +412,17 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
                 tiler_scatter_kernel<float><<<grid_for(h, nnz, 256), 256, 0, h->stream>>>(
                     nnz, ci, (const float*)out->row_val, tmp_t, tmp_rp, nullptr, out->tile_nnz,
                     out->tile_csr_Ptr, (float*)out->tile_csr_Val, out->tile_csr_Col, 1);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
     } else {
         // CSC tile order = stable sort of row-major tiles by tile column
         uint32_t *keys = nullptr, *perm = nullptr;
         int* row_to_csc = nullptr;
         int* cnt_csc = nullptr;
-        SPG_TRY(spg_alloc_t(h, &keys, (size_t)numtile + 1));
-        SPG_TRY(spg_alloc_t(h, &perm, (size_t)numtile + 1));
-        SPG_TRY(spg_alloc_t(h, &row_to_csc, (size_t)numtile + 1));
-        SPG_TRY(spg_alloc_t(h, &cnt_csc, (size_t)numtile + 1));
+        SPG_TRY(sc.alloc(&keys, (size_t)numtile + 1));
+        SPG_TRY(sc.alloc(&perm, (size_t)numtile + 1));
+        SPG_TRY(sc.alloc(&row_to_csc, (size_t)numtile + 1));
+        SPG_TRY(sc.alloc(&cnt_csc, (size_t)numtile + 1));
         SPG_TRY(spg_alloc_t(h, &out->csc_tile_ptr, (size_t)tilen + 1));
         SPG_TRY(spg_alloc_t(h, &out->csc_tile_rowidx, (size_t)numtile + 1));
         SPG_TRY(spg_alloc_t(h, &out->csc_to_row, (size_t)numtile + 1));
@@ -432,25 +432,24 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
             SPG_CUDA(h, cudaMemcpyAsync(keys, out->tile_columnidx, sizeof(int) * (size_t)numtile,
                                         cudaMemcpyDeviceToDevice, h->stream));
             iota_kernel<<<grid_for(h, numtile, 256), 256, 0, h->stream>>>(perm, numtile);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
             int bits = 1;
             while (bits < 31 && (1LL << bits) < tilen) bits++;
             SPG_TRY(spg_radix_sort_pairs(h, keys, perm, numtile, bits));
         }
         int* hist = nullptr;
-        SPG_TRY(spg_alloc_t(h, &hist, (size_t)tilen + 1));
+        SPG_TRY(sc.alloc(&hist, (size_t)tilen + 1));
         SPG_CUDA(h, cudaMemsetAsync(hist, 0, sizeof(int) * ((size_t)tilen + 1), h->stream));
         if (numtile > 0) {
             hist_kernel<<<grid_for(h, numtile, 256), 256, 0, h->stream>>>(out->tile_columnidx, numtile, hist);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
         SPG_TRY(spg_scan_i32_to_i32(h, hist, out->csc_tile_ptr, tilen));
-        spg_free_async(h, hist);
         if (numtile > 0) {
             csc_gather_kernel<<<grid_for(h, numtile, 256), 256, 0, h->stream>>>(
                 numtile, perm, tile_rowof, cnt_row, ptr_row, mask_row, out->csc_tile_rowidx, out->csc_to_row,
                 row_to_csc, cnt_csc, out->tile_csr_Ptr, out->mask);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
         SPG_TRY(spg_scan_i32_to_i32(h, cnt_csc, out->tile_nnz, numtile));
         if (nnz > 0) {
@@ -462,7 +461,7 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
                 tiler_scatter_kernel<float><<<grid_for(h, nnz, 256), 256, 0, h->stream>>>(
                     nnz, ci, (const float*)out->row_val, tmp_t, tmp_rp, row_to_csc, out->tile_nnz,
                     out->tile_csr_Ptr, (float*)out->tile_csr_Val, out->tile_csr_Col, 0);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
         if (flags & SPG_TILE_WITH_TILE_CSC) {
             SPG_TRY(spg_alloc_t(h, &out->tile_csc_Ptr, (size_t)numtile * TS + 16));
@@ -478,18 +477,8 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
                 tile_csc_kernel<float><<<grid_for(h, numtile, 128), 128, 0, h->stream>>>(
                     numtile, out->tile_nnz, out->tile_csr_Ptr, out->mask, (const float*)out->tile_csr_Val,
                     out->tile_csc_Ptr, out->tile_csc_Row, (float*)out->tile_csc_Val);
-            SPG_CUDA(h, cudaGetLastError());
+            SPG_LAUNCHED(h);
         }
-        spg_free_async(h, keys);
-        spg_free_async(h, perm);
-        spg_free_async(h, row_to_csc);
-        spg_free_async(h, cnt_csc);
     }
-    spg_free_async(h, tile_rowof);
-    spg_free_async(h, tmp_t);
-    spg_free_async(h, tmp_rp);
-    spg_free_async(h, ptr_row);
-    spg_free_async(h, mask_row);
-    spg_free_async(h, cnt_row);
     return spg_check_flags(h, "tiling");
 }

@@ -134,7 +134,7 @@ typedef struct {
     int64_t tensor_pairs;       /* tile pairs computed on tensor cores         */
     int64_t fp64_tiles;         /* C tiles recomputed in FP64                  */
     int32_t algo_used;          /* spg_algo the symbolic phase ran             */
-    int32_t reserved;
+    int32_t sizing_fallbacks;   /* step 1 ran exact because the learned slots did not fit */
     int64_t predicted_tiles;    /* C tile capacity from the sizing model (0: none) */
 } spg_stats;
 
@@ -147,6 +147,10 @@ spg_status spg_destroy(spg_handle_t h);
 spg_status spg_set_stream(spg_handle_t h, void* stream);
 const char* spg_last_error(spg_handle_t h);
 spg_status spg_get_stats(spg_handle_t h, spg_stats* out);
+/* Kernels this handle has launched since spg_create (a running count, so the
+   difference of two reads counts the launches of the calls between them).
+   No reference counterpart. */
+spg_status spg_kernel_launches(spg_handle_t h, int64_t* out);
 
 /* ---- tiling ----------------------------------------------------------------
  * Replaces csr2tile (src/tile_format.h:93-222), build_csc_tiles
@@ -295,7 +299,8 @@ spg_status spg_ctiles_to_csr_noalloc(spg_handle_t h, const spg_ctiles* C, int* o
    counterpart; it chains two of the reference's SpGEMMs): A (m x m) and P
    (m x nc) are device CSR; A*P is formed, converted to CSR and re-tiled as the
    B operand, P^T comes from spg_csr_transpose.  *products_out receives the
-   intermediate products of both SpGEMMs. */
+   intermediate products of both SpGEMMs; spg_get_stats afterwards sums the
+   two products' statistics (step times, counts). */
 spg_status spg_galerkin(spg_handle_t h, int m, int nc, int64_t nnzA, const int* A_rp, const int* A_ci,
                         const void* A_val, int64_t nnzP, const int* P_rp, const int* P_ci, const void* P_val,
                         spg_dtype dtype, spg_algo algo, spg_precision prec, spg_ctiles* RAP,

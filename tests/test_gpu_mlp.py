@@ -87,3 +87,56 @@ def test_underprediction_reruns_exactly(handle):
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
     assert st["overflow_reruns"] >= 1
     m.free()
+
+
+def test_overprediction_is_clamped_to_the_rows_bound(handle):
+    """A wildly over-predicting model (margin 1e6) asks for no more staging
+    than each tile-row can fill: its slot is clamped to the fewer of B's tile
+    columns, the tile pairs it reaches and the span they cover.  The
+    structure stays exact and no row re-runs."""
+    model = api.SizingModel.load(handle) if os.path.exists(api.SIZING_MODEL_PATH) else None
+    if model is None:
+        pytest.skip("no trained sizing model shipped")
+    a = synth.rmat(14, 16)
+    ref, _ = _run(handle, a)
+    got, st = _run(handle, a, model, margin=1e6)
+    for k in KEYS:
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    assert st["overflow_reruns"] == 0 and st["sizing_fallbacks"] == 0
+    # the clamp: per tile-row min(tilenB, tile pairs, column span) + 2 (rounding slack)
+    import oracle
+    T = oracle.csr2tile(a)
+    tp, tc = T["tile_ptr"].astype(np.int64), T["tile_columnidx"]
+    btiles = np.diff(tp)
+    bound = 0
+    for i in range(T["tilem"]):
+        ks = tc[tp[i]:tp[i + 1]]
+        if ks.size == 0:
+            bound += 2
+            continue
+        pairs = int(btiles[ks].sum())
+        nz = btiles[ks] > 0
+        span = int(tc[tp[ks[nz] + 1] - 1].max() - tc[tp[ks[nz]]].min() + 1) if nz.any() else 0
+        bound += min(T["tilen"], int(np.ceil(min(pairs, span) * 1.0001 + 2)))
+    assert got["numtileC"] <= st["predicted_tiles"] <= bound + T["tilem"], (st["predicted_tiles"], bound)
+    model.free()
+
+
+def test_staging_over_budget_falls_back_to_exact_two_pass(handle, monkeypatch):
+    """When the predicted slots exceed the staging budget (forced here to 16
+    bytes) the sized pass gives up before allocating and step 1 runs the
+    exact two passes: same structure, one fallback counted."""
+    if not os.path.exists(api.SIZING_MODEL_PATH):
+        pytest.skip("no trained sizing model shipped")
+    model = api.SizingModel.load(handle)
+    a = synth.rmat(13, 16)
+    ref, _ = _run(handle, a)
+    monkeypatch.setenv("SPG_SLOT_BUDGET_BYTES", "16")
+    got, st = _run(handle, a, model, margin=1.0)
+    for k in KEYS:
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    assert st["sizing_fallbacks"] == 1
+    monkeypatch.delenv("SPG_SLOT_BUDGET_BYTES")
+    got2, st2 = _run(handle, a, model, margin=1.0)
+    assert st2["sizing_fallbacks"] == 0 and st2["predicted_tiles"] > 0
+    model.free()
