@@ -6,18 +6,27 @@ U[-1,1] -- the configuration the metric is quoted on.  A "step" is one full
 SpGEMM (C tile structure + bitmask symbolic + numeric, with every allocation
 of C) on tiles already resident in HBM; GFLOP/s = 2 * products / step time,
 products = sum over A's nonzeros of nnz(B row) (src/spgemm_raw_v2.cu:95-99,250).
+Other workloads (--workload): poisson2d, stencil27, galerkin128 (the Galerkin
+triple product P^T (A P) on a 128^3 Poisson problem, one step = one
+spg_galerkin call), rmatNN, erbatch.
 
 Printed JSON (rank 0, one line) carries:
   value      GFLOP/s of the device-resident steps (max over ranks of the time)
   e2e        the same metric through the public C ABI with host buffers: each
              step copies the CSR inputs host->device, tiles them, multiplies and
-             copies every array of C back to pinned host memory
+             copies C's result arrays back to pinned host memory
   roofline   the dominant kernel's algorithmic bytes / its CUDA-event time
+  accuracy   C checked against the FP64 oracle: exact structure and relative
+             Frobenius error on sampled tile-rows (the hub rows first)
+  vs_plain   the same product by the plain per-C-tile kernels (the reference's
+             method, exact two-pass step 1, no sizing model) and by the default
+             path without the sizing model, timed in the same run
   cpu_baseline  OpenMP Gustavson (the CPU oracle's port of the reference's
              check, src/spgemm_raw_v2.cu:289-338) on a seeded row sample
 
-`--impl reference` times the reference's CPU implementation of the path (that
-Gustavson port) on all host threads for the same workload and metric.
+`config` holds only what identifies the workload, so both arms print the same
+one.  `--impl reference` times the reference's CPU implementation of the path
+(that Gustavson port) on all host threads for the same workload and metric.
 """
 from __future__ import annotations
 
@@ -39,28 +48,93 @@ from gpu_spgemm_gb300 import synth  # noqa: E402
 L2_BYTES = 129 * 1024 * 1024
 TS = 16
 
-# DRAM bytes per launch of the dominant kernel, from one-pass ncu captures of
-# the same bench command (dram__bytes_read.sum + dram__bytes_write.sum), by
-# (workload, step); profiles/traffic_rmat20.md holds the capture.
-MEASURED_TRAFFIC = {("rmat20", "step3"): 279.02e9 + 65.14e9}
+# DRAM traffic of the numeric kernel per algorithmic byte, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum of rw_numeric_kernel) on the
+# R-MAT 2^17 product, where the capture holds a few GB; the full-size launch's
+# traffic is this ratio times its algorithmic bytes.
+TRAFFIC_PER_ALGO_BYTE = {"rw_numeric_kernel": None}
 
 
-def workload(name: str):
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def workload(name: str) -> dict:
+    """kind "product": C = A*B; kind "galerkin": RAP = P^T (A P)."""
     if name == "rmat20":
         a = synth.rmat(20, 16)
-        return a, a, {"workload": "C=A*A, A=R-MAT scale 20, edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), "
-                                  "duplicates merged, FP32 U[-1,1]", "n": a.m, "nnz": a.nnz}
+        return dict(kind="product", a=a, b=a, desc="C=A*A, A=R-MAT scale 20, edge factor 16, "
+                                                   "(a,b,c,d)=(.57,.19,.19,.05), duplicates merged, FP32 U[-1,1]")
     if name == "poisson2d":
         a = synth.poisson2d(256)
-        return a, a, {"workload": "C=A*A, A=2-D 5-point Poisson 256x256, FP64", "n": a.m, "nnz": a.nnz}
+        return dict(kind="product", a=a, b=a, desc="C=A*A, A=2-D 5-point Poisson 256x256, FP64")
     if name == "stencil27":
         a = synth.stencil27_dof3(64)
-        return a, a, {"workload": "C=A*A, A=27-point stencil 64^3 x 3 dof, FP32 N(0,1)", "n": a.m, "nnz": a.nnz}
+        return dict(kind="product", a=a, b=a, desc="C=A*A, A=27-point stencil 64^3 x 3 dof, FP32 N(0,1)")
+    if name.startswith("galerkin"):
+        g = int(name[8:] or 128)
+        a = synth.poisson3d(g)
+        p = synth.smoothed_aggregation(a, synth.aggregation_p0(g))
+        return dict(kind="galerkin", a=a, p=p,
+                    desc=f"RAP=P^T(A P), A=3-D 7-point Poisson {g}^3, P=2x2x2 aggregation smoothed by one "
+                         "weighted-Jacobi step (omega=2/3), FP32")
     if name.startswith("rmat"):
         s = int(name[4:])
         a = synth.rmat(s, 16)
-        return a, a, {"workload": f"C=A*A, A=R-MAT scale {s}, edge factor 16, FP32", "n": a.m, "nnz": a.nnz}
+        return dict(kind="product", a=a, b=a, desc=f"C=A*A, A=R-MAT scale {s}, edge factor 16, FP32")
     raise SystemExit(f"unknown workload {name}")
+
+
+def galerkin_operands(w: dict):
+    """P^T and A*P as host CSR (structure and FP32 values from scipy), for the
+    product count and the CPU legs."""
+    if "pt" not in w:
+        a, p = w["a"], w["p"]
+        ap = (a.to_scipy().astype(np.float64) @ p.to_scipy().astype(np.float64)).tocsr()
+        w["pt"] = synth.transpose(p)
+        w["ap"] = synth.CSR.from_scipy(ap, dtype=np.float32)
+    return w["pt"], w["ap"]
+
+
+def structural_products(w: dict) -> int:
+    if w["kind"] == "product":
+        return synth.products(w["a"], w["b"])
+    pt, ap = galerkin_operands(w)
+    # A*P keeps every structural product (cancellations included), as the tiled
+    # product does; scipy's A@P drops exact zeros, so count on |A| |P|
+    a, p = w["a"], w["p"]
+    return synth.products(a, p) + synth.products(pt, structural_ap(w))
+
+
+def structural_ap(w: dict):
+    if "ap_struct" not in w:
+        a, p = w["a"], w["p"]
+        sa = a.to_scipy().astype(np.float64)
+        sp_ = p.to_scipy().astype(np.float64)
+        sa.data[:] = 1.0
+        sp_.data[:] = 1.0
+        w["ap_struct"] = synth.CSR.from_scipy((sa @ sp_).tocsr(), dtype=np.float32)
+    return w["ap_struct"]
+
+
+def workload_config(w: dict, products: int) -> dict:
+    """The workload's identity, the same in both arms' lines."""
+    if w["kind"] == "product":
+        a, b = w["a"], w["b"]
+        vbytes = a.val.dtype.itemsize
+        inputs = (a.nnz + b.nnz) * (4 + vbytes) + 4 * (a.m + b.m + 2)
+        cfg = {"workload": w["desc"], "n": a.m, "nnz": a.nnz, "products": int(products)}
+    else:
+        a, p = w["a"], w["p"]
+        inputs = (a.nnz + p.nnz) * 8 + 4 * (a.m + p.m + 2)
+        cfg = {"workload": w["desc"], "n": a.m, "nnz": a.nnz, "nnzP": p.nnz, "nc": p.n,
+               "products": int(products)}
+    cfg["l2"] = ("inputs exceed L2 (%.0f MB of CSR > 129 MB), no flush between steps" % (inputs / 1e6)
+                 if inputs > L2_BYTES else "L2 flushed between timed steps (256 MB write outside the timing)")
+    return cfg
+
+
+def needs_flush(w: dict) -> bool:
+    return "flushed" in workload_config(w, 0)["l2"]
 
 
 def tile_bytes(numtile, nnz, tilem, v, b_side=False):
@@ -148,63 +222,211 @@ def job_time_and_value(ms_local: float, flops_local: float, world: int, device) 
     return ms, float(f.item()) / (ms * 1e-3) / 1e9
 
 
-def cpu_gflops(a, b, target_s: float = 12.0, dtype=np.float32):
-    """OpenMP Gustavson on a seeded stride sample of A's rows, sized to about
-    target_s seconds; returns (GFLOP/s, threads, sample description)."""
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle's OpenMP Gustavson: a reported baseline, never the product)
+# ---------------------------------------------------------------------------
+def _row_sample(a, k, off):
+    rows = np.arange(off, a.m, k, dtype=np.int64)
+    lens = np.diff(a.row_ptr)[rows]
+    rp = np.zeros(rows.size + 1, np.int64)
+    np.cumsum(lens, out=rp[1:])
+    starts = a.row_ptr[rows].astype(np.int64)
+    idx = np.repeat(starts - rp[:-1], lens) + np.arange(int(rp[-1]), dtype=np.int64) if rows.size else \
+        np.zeros(0, np.int64)
+    return synth.CSR(rows.size, a.n, rp.astype(np.int32), a.col_idx[idx], a.val[idx])
+
+
+def cpu_gflops(w: dict, target_s: float = 12.0):
+    """OpenMP Gustavson on a seeded stride sample of the left operand's rows,
+    sized to about target_s seconds; returns (GFLOP/s, threads, sample text).
+    For the Galerkin workload both products are sampled alike."""
     import oracle
     threads = oracle.max_threads()
     rng = np.random.Generator(np.random.PCG64(0xC0FFEE))
+    if w["kind"] == "product":
+        legs = [(w["a"], w["b"])]
+    else:
+        pt, ap = galerkin_operands(w)
+        legs = [(w["a"], w["p"]), (pt, ap)]
+    dtype = np.float64 if legs[0][0].val.dtype == np.float64 else np.float32
 
-    def sample(frac):
+    def run(frac):
         k = max(1, int(round(1.0 / frac)))
         off = int(rng.integers(0, k))
-        rows = np.arange(off, a.m, k, dtype=np.int64)
-        lens = np.diff(a.row_ptr)[rows]
-        rp = np.zeros(rows.size + 1, np.int64)
-        np.cumsum(lens, out=rp[1:])
-        idx = np.concatenate([np.arange(a.row_ptr[r], a.row_ptr[r + 1]) for r in rows]) if rows.size else \
-            np.zeros(0, np.int64)
-        s = synth.CSR(rows.size, a.n, rp.astype(np.int32), a.col_idx[idx], a.val[idx].astype(dtype))
-        return s, k
+        prods, dt = 0, 0.0
+        for left, right in legs:
+            s = _row_sample(left, k, off)
+            prods += synth.products(s, right)
+            t0 = time.perf_counter()
+            oracle.gustavson_rows(s, right, 0, s.m, dtype)
+            dt += time.perf_counter() - t0
+        return k, prods, max(dt, 1e-4)
 
-    frac = 0.01
-    s, k = sample(frac)
-    p = synth.products(s, b)
-    t0 = time.perf_counter()
-    oracle.gustavson_rows(s, b, 0, s.m, dtype)
-    dt = max(time.perf_counter() - t0, 1e-4)
-    frac = min(1.0, frac * target_s / dt)
-    s, k = sample(frac)
-    p = synth.products(s, b)
-    t0 = time.perf_counter()
-    oracle.gustavson_rows(s, b, 0, s.m, dtype)
-    dt = time.perf_counter() - t0
-    return 2.0 * p / dt / 1e9, threads, f"every {k}-th row of A ({s.m} rows, {p} products), {dt:.1f} s"
+    k, p, dt = run(0.01)
+    frac = min(1.0, 0.01 * target_s / dt)
+    k, p, dt = run(frac)
+    what = "left operand" if w["kind"] == "product" else "left operand of each product"
+    return 2.0 * p / dt / 1e9, threads, f"every {k}-th row of the {what} ({p} products), {dt:.1f} s"
 
 
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    a, b, cfg = workload(args.workload)
+    w = workload(args.workload)
     import oracle
-    dtype = np.float64 if a.val.dtype == np.float64 else np.float32
+    products = structural_products(w)
+    dtype = np.float64 if w["a"].val.dtype == np.float64 else np.float32
     vals = []
     desc = ""
     threads = oracle.max_threads()
     for i in range(args.warmup + args.steps):
-        g, threads, desc = cpu_gflops(a, b, target_s=args.ref_step_s, dtype=dtype)
+        g, threads, desc = cpu_gflops(w, target_s=args.ref_step_s)
         if i >= args.warmup:
             vals.append(g)
     v = statistics.mean(vals)
     line = {"impl": "reference", "metric": "SpGEMM GFLOP/s", "value": v, "unit": "GFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": np.dtype(dtype).name,
-            "data": "synthetic", "config": cfg, "vs_baseline": None,
+            "data": "synthetic", "config": workload_config(w, products), "vs_baseline": None,
             "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": threads, "kind": "port",
                              "sample": "OpenMP row-parallel Gustavson (CPU oracle's restatement of "
                                        "src/spgemm_raw_v2.cu:289-338), " + desc},
             "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+class Timer:
+    """CUDA-event timing of K steps on the library's stream: one bracket when
+    the inputs exceed L2, else one bracket per step with an L2 flush (a 256 MB
+    write on the same stream) between steps, outside the brackets."""
+
+    def __init__(self, stream, flush: bool):
+        import torch
+        self.torch = torch
+        self.stream = stream
+        self.flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if flush else None
+
+    def run(self, fn, steps: int) -> float:
+        torch = self.torch
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        if self.flush_buf is None:
+            torch.cuda.synchronize()
+            ev[0].record(self.stream)
+            for _ in range(steps):
+                fn()
+            ev[1].record(self.stream)
+            torch.cuda.synchronize()
+            return ev[0].elapsed_time(ev[1]) / steps
+        tot = 0.0
+        for _ in range(steps):
+            with torch.cuda.stream(self.stream):
+                self.flush_buf.fill_(1)
+            torch.cuda.synchronize()
+            ev[0].record(self.stream)
+            fn()
+            ev[1].record(self.stream)
+            torch.cuda.synchronize()
+            tot += ev[0].elapsed_time(ev[1])
+        return tot / steps
+
+
+def load_peaks():
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        peaks = {}
+    if "hbm_gbs" in peaks:
+        return float(peaks["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sized):
+    """Roofline of the dominant step's kernel: its algorithmic bytes (each
+    array it must touch, read or written once) over its CUDA-event time."""
+    hbm_peak, peak_src = load_peaks()
+    a_b = tile_bytes(A.numtile, A.nnz, A.tilem, v)
+    b_b = tile_bytes(B.numtile, B.nnz, B.tilem, v, b_side=True)
+    # numeric: reads A and B (tiles and row views alike: the same bytes once),
+    # C's structure; writes C's values and column bytes
+    num_bytes = a_b + b_b + 4 * (A.tilem + 1) + numtileC * (4 + 4 + 8 + 32 + 16) + nnzC * (v + 1)
+    sym_bytes = (4 * (A.tilem + 1) + A.numtile * (4 + 4 + 16) + A.nnz + B.numtile * (4 + 32) + 4 * (B.tilen + 1)
+                 + numtileC * (4 + 4 + 32 + 16 + 4))
+    st1_bytes = 4 * (A.tilem + 1) * 2 + 4 * A.numtile + 4 * B.numtile + 8 * numtileC
+    steps_ms = {"step1": s1, "step2": s2, "step3": s3}
+    dom = max(steps_ms, key=steps_ms.get)
+    dom_bytes = {"step1": st1_bytes, "step2": sym_bytes, "step3": num_bytes}[dom]
+    names = {"step1": "c1_slot_kernel + c1_compact_kernel" if sized else "c1_count_kernel + c1_fill_kernel",
+             "step2": "rw_symbolic_kernel" if rowwise else "c2_symbolic_kernel",
+             "step3": "rw_numeric_kernel" if rowwise else "c3_numeric_kernel"}
+    achieved = dom_bytes / (steps_ms[dom] * 1e-3) / 1e9
+    traffic = args.traffic
+    traffic_src = "--traffic" if traffic is not None else None
+    ratio = TRAFFIC_PER_ALGO_BYTE.get(names[dom].split(" ")[0])
+    if traffic is None and ratio is not None:
+        traffic = ratio * dom_bytes
+        traffic_src = "ncu DRAM bytes per algorithmic byte on the R-MAT 2^17 launch, times this launch's bytes"
+    return {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_source": peak_src, "algorithmic_bytes": dom_bytes,
+            "ms": steps_ms[dom], "traffic": traffic, "traffic_source": traffic_src}, a_b + b_b
+
+
+def check_ranges(tilem, which="default"):
+    """Tile-rows checked against the oracle: the first 512 (the hub rows of a
+    power-law matrix, the worst case for accumulation order) and 2,048 from
+    the middle."""
+    r = [(0, min(tilem, 512))]
+    mid = tilem // 2
+    if mid + 2048 <= tilem and mid >= 512:
+        r.append((mid, mid + 2048))
+    return r
+
+
+def value_check(h, api, w, Cm):
+    """C's structure and values on sampled tile-rows against the FP64 oracle
+    (each C tile-row depends only on the same 16 rows of A and all of B): the
+    oracle forms those rows by Gustavson in FP64 and compares entry by entry.
+    Returns the relative Frobenius error, the structural mismatches and what
+    was checked."""
+    import ctypes as C
+    import oracle
+    a, b = w["a"], w["b"]
+    vd = np.float64 if a.val.dtype == np.float64 else np.float32
+    tp = np.zeros(Cm.tilem + 1, np.int32)
+    h.check(h.lib.spg_ctiles_to_host(h.h, C.byref(Cm.c), tp.ctypes.data, None, None, None, None, None, None, None))
+    err2 = ref2 = 0.0
+    bad = 0
+    nvals = 0
+    rows = 0
+    t0 = time.perf_counter()
+    for i0, i1 in check_ranges(Cm.tilem):
+        s, e = int(tp[i0]), int(tp[i1])
+        nt = e - s
+        d = dict(tile_colidxC=np.zeros(max(nt, 1), np.int32), maskC=np.zeros(max(nt, 1) * 16, np.uint16),
+                 tile_nnzC=np.zeros(nt + 1, np.int64), ptrRowC=np.zeros(max(nt, 1) * 16, np.uint8))
+        h.check(h.lib.spg_ctiles_to_host_range(h.h, C.byref(Cm.c), s, e, None, d["tile_colidxC"].ctypes.data,
+                                               d["maskC"].ctypes.data, d["tile_nnzC"].ctypes.data,
+                                               d["ptrRowC"].ctypes.data, None, None, 0, None))
+        nv = int(d["tile_nnzC"][-1] - d["tile_nnzC"][0])
+        d["tile_valC"] = np.zeros(max(nv, 1), vd)
+        d["tile_colC"] = np.zeros(max(nv, 1), np.uint8)
+        got = C.c_int64()
+        h.check(h.lib.spg_ctiles_to_host_range(h.h, C.byref(Cm.c), s, e, None, None, None, None, None,
+                                               d["tile_valC"].ctypes.data, d["tile_colC"].ctypes.data, max(nv, 1),
+                                               C.byref(got)))
+        d["tile_ptr"] = tp[i0:i1 + 1].astype(np.int64) - s
+        r = oracle.check_tilerows(a, b, i0, i1, d)
+        err2 += (r["rel_frob"] * r["ref_frob"]) ** 2
+        ref2 += r["ref_frob"] ** 2
+        bad += r["mismatches"]
+        nvals += nv
+        rows += i1 - i0
+    return {"tile_rows_checked": rows, "ranges": check_ranges(Cm.tilem), "c_values_checked": nvals,
+            "rel_frob_vs_fp64": float(np.sqrt(err2) / (np.sqrt(ref2) or 1.0)), "structure_mismatches": bad,
+            "cols_equal": bad == 0, "oracle": "FP64 Gustavson per row (src/spgemm_raw_v2.cu:289-338)",
+            "check_s": round(time.perf_counter() - t0, 1)}
 
 
 def run_ours(args):
@@ -214,8 +436,11 @@ def run_ours(args):
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
+    w = workload(args.workload)
+    if w["kind"] == "galerkin":
+        return run_galerkin(args, w, world, rank, local)
     from gpu_spgemm_gb300 import api
-    a, b, cfg = workload(args.workload)
+    a, b = w["a"], w["b"]
     dtype = a.val.dtype
     v = 8 if dtype == np.float64 else 4
     stream = torch.cuda.Stream()
@@ -229,13 +454,21 @@ def run_ours(args):
     if args.sizing and os.path.exists(api.SIZING_MODEL_PATH):
         sizing = api.SizingModel.load(h)
         sizing.attach(args.sizing_margin)
+    timer = Timer(stream, needs_flush(w))
 
-    def step():
-        C = api.spgemm(h, A, B, algo=args.algo, prec=args.prec)
-        st = h.stats()
-        info = (C.numtileC, C.nnzC, C.pairs)
+    last = {}
+
+    def step(algo=args.algo, prec=args.prec):
+        C = api.spgemm(h, A, B, algo=algo, prec=prec)
+        last["stats"] = h.stats()
+        last["info"] = (C.numtileC, C.nnzC, C.pairs)
         C.free()
-        return st, info
+
+    stats = []
+
+    def timed_step():
+        step()
+        stats.append(last["stats"])
 
     for _ in range(args.warmup):
         step()
@@ -244,130 +477,260 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    stats = []
-    info = None
-    for _ in range(args.steps):
-        st, info = step()
-        stats.append(st)
-    ev1.record(stream)
-    torch.cuda.synchronize()
+    l0 = h.launches()
+    ms_local = timer.run(timed_step, args.steps)
+    launches = h.launches() - l0
     clk = clocks.stop()
-    ms, value = job_time_and_value(ev0.elapsed_time(ev1) / args.steps, flops, world, "cuda")
-    numtileC, nnzC, pairs = info
-
-    # ---- roofline of the dominant kernel (CUDA events around it inside the library)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    ms, value = job_time_and_value(ms_local, flops, world, "cuda")
+    numtileC, nnzC, pairs = last["info"]
     s1 = statistics.mean(s["ms_step1"] for s in stats)
     s2 = statistics.mean(s["ms_step2"] for s in stats)
     s3 = statistics.mean(s["ms_step3"] for s in stats)
-    a_b = tile_bytes(A.numtile, A.nnz, A.tilem, v)
-    b_b = tile_bytes(B.numtile, B.nnz, B.tilem, v, b_side=True)
-    c_b = c_bytes(numtileC, nnzC, A.tilem, v)
-    # numeric kernel: reads A and B tiles and C's structure, writes C's values and column bytes
-    num_bytes = (a_b + b_b + 4 * (A.tilem + 1) + numtileC * (4 + 4 + 8 + 32 + 16) + nnzC * (v + 1))
-    sym_bytes = (4 * (A.tilem + 1) + A.numtile * (4 + 4 + 16) + A.nnz + B.numtile * (4 + 32) + 4 * (B.tilen + 1)
-                 + numtileC * (4 + 4 + 32 + 16 + 4))
-    steps_ms = {"step1": s1, "step2": s2, "step3": s3}
-    dom = max(steps_ms, key=steps_ms.get)
-    dom_bytes = {"step1": 4 * (A.tilem + 1) * 2 + 4 * A.numtile + 4 * B.numtile + 8 * numtileC,
-                 "step2": sym_bytes, "step3": num_bytes}[dom]
-    achieved = dom_bytes / (steps_ms[dom] * 1e-3) / 1e9
     rowwise = stats[-1].get("algo_used", 1) == 2
-    names = {"step1": "c1_slot_kernel + c1_compact_kernel" if args.sizing else "c1_count_kernel + c1_fill_kernel",
-             "step2": "rw_symbolic_kernel" if rowwise else "c2_symbolic_kernel",
-             "step3": "rw_numeric_kernel" if rowwise else "c3_numeric_kernel"}
-    roofline = {"bound": "hbm", "kernel": names[dom],
-                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "peak_source": peak_src, "algorithmic_bytes": dom_bytes, "ms": steps_ms[dom],
-                "traffic": args.traffic if args.traffic is not None else MEASURED_TRAFFIC.get((args.workload, dom))}
-    total_bytes = a_b + b_b + c_b
-    hbm_steps = total_bytes / (ms * 1e-3) / 1e9
+    roofline, ab_bytes = step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sizing is not None)
+    c_b = c_bytes(numtileC, nnzC, A.tilem, v)
 
-    accuracy = value_check(h, api, a, b, args) if args.check else None
+    accuracy = None
+    if not args.no_check:
+        Cm = api.spgemm(h, A, B, algo=args.algo, prec=args.prec)
+        accuracy = value_check(h, api, w, Cm)
+        accuracy.update(numtileC=Cm.numtileC, nnzC=Cm.nnzC, tensor_pairs=h.stats()["tensor_pairs"],
+                        fp64_tiles=h.stats()["fp64_tiles"])
+        Cm.free()
 
-    # ---- end to end through the public API with host buffers
+    # ---- the same product by the plain kernels and without the sizing model
+    vs_plain = None
+    if not args.no_compare:
+        vs_plain = {}
+        if sizing is not None:
+            sizing.detach()
+        step(algo="plain", prec="f32")  # warm-up
+        pms = timer.run(lambda: step(algo="plain", prec="f32"), args.plain_steps)
+        ps = last["stats"]
+        vs_plain["plain"] = {"gflops": flops / (pms * 1e-3) / 1e9, "ms_step": pms, "ms_step1": ps["ms_step1"],
+                             "ms_step2": ps["ms_step2"], "ms_step3": ps["ms_step3"],
+                             "what": "per-C-tile kernels (tile-list intersection, register accumulation; the "
+                                     "reference's method), exact two-pass step 1, no sizing model, FP32 registers"}
+        if sizing is not None:
+            step()
+            nms = timer.run(step, max(1, args.steps // 2))
+            ns = last["stats"]
+            vs_plain["default_without_sizing_model"] = {
+                "gflops": flops / (nms * 1e-3) / 1e9, "ms_step": nms, "ms_step1": ns["ms_step1"],
+                "ms_step2": ns["ms_step2"], "ms_step3": ns["ms_step3"]}
+            vs_plain["sizing_model_gain"] = nms / ms_local
+            sizing.attach(args.sizing_margin)
+        vs_plain["speedup_vs_plain"] = pms / ms_local
+
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(h, api, a, b, args, flops, stream)
 
-    # ---- CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        g, thr, desc = cpu_gflops(a, b, target_s=args.cpu_s, dtype=np.float64 if v == 8 else np.float32)
+        g, thr, desc = cpu_gflops(w, target_s=args.cpu_s)
         cpu = {"value": g, "unit": "GFLOP/s", "cores": thr, "kind": "port",
                "sample": "OpenMP row-parallel Gustavson (CPU oracle's restatement of "
                          "src/spgemm_raw_v2.cu:289-338), " + desc}
 
     if rank == 0:
-        cfg = dict(cfg)
-        cfg.update({"products": products, "numtileC": numtileC, "nnzC": nnzC, "tile_pairs": pairs,
-                    "algo": args.algo, "prec": args.prec,
-                    "l2": "inputs and outputs exceed L2 (A,B tiles %.2f GB, C %.1f GB > 129 MB)" %
-                          ((a_b + b_b) / 1e9, c_b / 1e9),
-                    "ms_step1": s1, "ms_step2": s2, "ms_step3": s3,
-                    "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak,
-                    "tensor_pairs": stats[-1].get("tensor_pairs", 0), "fp64_tiles": stats[-1].get("fp64_tiles", 0),
-                    "learned_sizing": None if sizing is None else {
-                        "model": os.path.relpath(api.SIZING_MODEL_PATH, ROOT), "margin": args.sizing_margin,
-                        "predicted_tiles": stats[-1].get("predicted_tiles", 0), "actual_tiles": numtileC,
-                        "overflow_reruns": stats[-1].get("overflow_reruns", 0),
-                        "step1": "one bitmap pass into predicted per-row slots, then compaction; "
-                                 "rows that outgrow their slot re-run the exact fill"},
-                    "accuracy": accuracy})
+        hbm_peak = roofline["peak"]
+        hbm_steps = (ab_bytes + c_b) / (ms * 1e-3) / 1e9
+        details = {"numtileC": numtileC, "nnzC": nnzC, "tile_pairs": pairs, "algo": args.algo, "prec": args.prec,
+                   "algo_used": {0: "auto", 1: "plain", 2: "rowwise"}.get(stats[-1].get("algo_used"), "?"),
+                   "ms_step1": s1, "ms_step2": s2, "ms_step3": s3,
+                   "tile_bytes": {"A+B": ab_bytes, "C": c_b},
+                   "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak,
+                   "tensor_pairs": stats[-1].get("tensor_pairs", 0), "fp64_tiles": stats[-1].get("fp64_tiles", 0),
+                   "learned_sizing": None if sizing is None else {
+                       "model": os.path.relpath(api.SIZING_MODEL_PATH, ROOT), "margin": args.sizing_margin,
+                       "predicted_tiles": stats[-1].get("predicted_tiles", 0), "actual_tiles": numtileC,
+                       "overflow_reruns": stats[-1].get("overflow_reruns", 0),
+                       "fallbacks": stats[-1].get("sizing_fallbacks", 0),
+                       "step1": "one bitmap pass into predicted per-row slots, then compaction; "
+                                "rows that outgrow their slot re-run the exact fill"}}
         line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": np.dtype(dtype).name, "data": "synthetic",
-                "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-                "gpu_launches": gpu_launches(args.algo) * args.steps}
+                "config": workload_config(w, products), "details": details, "accuracy": accuracy,
+                "vs_plain": vs_plain, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     h.close()
     if world > 1:
         dist.destroy_process_group()
 
 
-def value_check(h, api, a, b, args, tile_rows=512):
-    """Relative Frobenius error of C's values against the FP64 oracle on the
-    first `tile_rows` C tile-rows (each C tile-row depends only on the same
-    16 rows of A, so the oracle multiplies that row block of A by B)."""
-    import ctypes as C
+def run_galerkin(args, w, world, rank, local):
+    """RAP = P^T (A P) through spg_galerkin: A and P resident as device CSR;
+    one step tiles A and P, forms A*P, expands it to CSR and re-tiles it as
+    the B operand, transposes P, tiles P^T and forms P^T (A P).  GFLOP/s
+    counts both products."""
+    import torch
+    import torch.distributed as dist
+    from gpu_spgemm_gb300 import api
     import oracle
-    from gpu_spgemm_gb300 import _lib as L
-    rows = min(a.m, 16 * tile_rows)
-    asub = synth.CSR(rows, a.n, a.row_ptr[:rows + 1].copy(), a.col_idx[:a.row_ptr[rows]].copy(),
-                     a.val[:a.row_ptr[rows]].copy())
-    S = oracle.spgemm_tiles(asub, b)
-    A = api.csr2tile(h, a)
-    B = api.build_csc_tiles(h, b)
-    Cm = api.spgemm(h, A, B, algo=args.algo, prec=args.prec)
-    nt = int(S["numtileC"])
-    nv = int(S["nnzC"])
-    vd = np.float64 if a.val.dtype == np.float64 else np.float32
-    vals = np.zeros(max(nv, 1), vd)
-    cols = np.zeros(max(nv, 1), np.uint8)
-    got = C.c_int64()
-    h.check(h.lib.spg_ctiles_to_host_range(h.h, C.byref(Cm.c), 0, nt, None, None, None, None, None,
-                                           vals.ctypes.data, cols.ctypes.data, max(nv, 1), C.byref(got)))
-    st = h.stats()
-    Cm.free(); A.free(); B.free()
-    ref = S["tile_valC"]
-    err = float(np.linalg.norm(vals[:nv].astype(np.float64) - ref) / (np.linalg.norm(ref) or 1.0))
-    return {"tile_rows_checked": int(rows // 16), "c_values_checked": nv, "rel_frob_vs_fp64": err,
-            "cols_equal": bool(np.array_equal(cols[:nv], S["tile_colC"])), "tensor_pairs": st["tensor_pairs"],
-            "fp64_tiles": st["fp64_tiles"]}
+    a, p = w["a"], w["p"]
+    stream = torch.cuda.Stream()
+    h = api.Handle(local, stream)
+    dev = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    ar, ac, av = dev(a.row_ptr), dev(a.col_idx), dev(a.val)
+    pr_, pc, pv = dev(p.row_ptr), dev(p.col_idx), dev(p.val)
+    sizing = None
+    if args.sizing and os.path.exists(api.SIZING_MODEL_PATH):
+        sizing = api.SizingModel.load(h)
+        sizing.attach(args.sizing_margin)
+    timer = Timer(stream, needs_flush(w))
+    last = {}
+
+    def step(algo=args.algo, prec=args.prec):
+        Cm, prods = api.galerkin_device(h, a.m, p.n, a.nnz, ar.data_ptr(), ac.data_ptr(), av.data_ptr(), p.nnz,
+                                        pr_.data_ptr(), pc.data_ptr(), pv.data_ptr(), a.val.dtype, algo, prec)
+        last.update(prods=prods, stats=h.stats(), info=(Cm.numtileC, Cm.nnzC))
+        return Cm
+
+    stats = []
+
+    def timed_step():
+        step().free()
+        stats.append(last["stats"])
+
+    for _ in range(args.warmup):
+        step().free()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = h.launches()
+    ms_local = timer.run(timed_step, args.steps)
+    launches = h.launches() - l0
+    clk = clocks.stop()
+    products = last["prods"]
+    flops = 2.0 * products
+    ms, value = job_time_and_value(ms_local, flops, world, "cuda")
+    st = stats[-1]
+    hbm_peak, peak_src = load_peaks()
+
+    accuracy = None
+    if not args.no_check:
+        Cm = step()
+        got = Cm.to_host()
+        Cm.free()
+        t0 = time.perf_counter()
+        S1 = oracle.spgemm_tiles(a, p)
+        rp, ci, vv = oracle.tiles_to_csr(a.m, p.n, S1)
+        ap = synth.CSR(a.m, p.n, rp.astype(np.int32), ci, vv)
+        S = oracle.spgemm_tiles(synth.transpose(p), ap)
+        bad = sum(int(not np.array_equal(got[k], S[k].astype(got[k].dtype)))
+                  for k in ("tile_ptrC", "tile_rowidxC", "tile_colidxC", "maskC", "tile_nnzC", "ptrRowC",
+                            "tile_colC"))
+        ref = S["tile_valC"]
+        err = float(np.linalg.norm(got["tile_valC"].astype(np.float64) - ref) / (np.linalg.norm(ref) or 1.0))
+        accuracy = {"rel_frob_vs_fp64": err, "structure_arrays_differing": bad, "cols_equal": bad == 0,
+                    "numtileC": int(got["numtileC"]), "nnzC": int(got["nnzC"]),
+                    "oracle": "tiled FP64 oracle: A*P, expanded to CSR, then P^T (A P)",
+                    "check_s": round(time.perf_counter() - t0, 1)}
+
+    vs_plain = None
+    if not args.no_compare:
+        if sizing is not None:
+            sizing.detach()
+        step(algo="plain", prec="f32").free()
+        pms = timer.run(lambda: step(algo="plain", prec="f32").free(), max(1, args.steps // 2))
+        vs_plain = {"plain": {"gflops": flops / (pms * 1e-3) / 1e9, "ms_step": pms,
+                              "what": "both products on the per-C-tile kernels, exact two-pass step 1, "
+                                      "no sizing model"},
+                    "speedup_vs_plain": pms / ms_local}
+        if sizing is not None:
+            step().free()
+            nms = timer.run(lambda: step().free(), max(1, args.steps // 2))
+            vs_plain["default_without_sizing_model"] = {"gflops": flops / (nms * 1e-3) / 1e9, "ms_step": nms}
+            vs_plain["sizing_model_gain"] = nms / ms_local
+            sizing.attach(args.sizing_margin)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = galerkin_e2e(h, api, w, args, flops, stream)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        g, thr, desc = cpu_gflops(w, target_s=args.cpu_s)
+        cpu = {"value": g, "unit": "GFLOP/s", "cores": thr, "kind": "port",
+               "sample": "OpenMP row-parallel Gustavson (CPU oracle's restatement of "
+                         "src/spgemm_raw_v2.cu:289-338) of A*P and P^T (A P), " + desc}
+    if rank == 0:
+        s123 = st["ms_step1"] + st["ms_step2"] + st["ms_step3"]
+        details = {"numtileC": last["info"][0], "nnzC": last["info"][1], "algo": args.algo, "prec": args.prec,
+                   "ms_steps_of_both_products": {"step1": st["ms_step1"], "step2": st["ms_step2"],
+                                                 "step3": st["ms_step3"]},
+                   "ms_tiling_and_conversions": ms_local - s123,
+                   "learned_sizing": None if sizing is None else {"margin": args.sizing_margin,
+                                                                  "overflow_reruns": st["overflow_reruns"]}}
+        steps_ms = {"step1": st["ms_step1"], "step2": st["ms_step2"], "step3": st["ms_step3"],
+                    "tiling and conversions": ms_local - s123}
+        dom = max(steps_ms, key=steps_ms.get)
+        roofline = {"bound": "hbm", "kernel": f"galerkin {dom}", "achieved": None, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": None, "peak_source": peak_src, "ms": steps_ms[dom], "traffic": None}
+        line = {"metric": "SpGEMM GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": np.dtype(a.val.dtype).name, "data": "synthetic",
+                "config": workload_config(w, products), "details": details, "accuracy": accuracy,
+                "vs_plain": vs_plain, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        dist.destroy_process_group()
 
 
-def gpu_launches(algo):
-    # plain path per step: step1 count + scan + i64->i32 + fill, step2 symbolic + scan, step3 numeric
-    return 7
+def galerkin_e2e(h, api, w, args, flops, stream):
+    """spg_galerkin end to end: A and P copied from pinned host memory to the
+    device each step, RAP's result arrays (the ones the reference reads back,
+    src/spgemm_raw_v2.cu:257-266) copied to pinned host memory."""
+    import ctypes as C
+    import torch
+    a, p = w["a"], w["p"]
+    pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+    host = [pin(x) for x in (a.row_ptr, a.col_idx, a.val, p.row_ptr, p.col_idx, p.val)]
+    devs = [torch.empty_like(x, device="cuda") for x in host]
+    h2d = sum(x.numel() * x.element_size() for x in host)
+    out = {}
+
+    def one():
+        with torch.cuda.stream(stream):
+            for d, x in zip(devs, host):
+                d.copy_(x, non_blocking=True)
+        ar, ac, av, pr_, pc, pv = devs
+        Cm, _ = api.galerkin_device(h, a.m, p.n, a.nnz, ar.data_ptr(), ac.data_ptr(), av.data_ptr(), p.nnz,
+                                    pr_.data_ptr(), pc.data_ptr(), pv.data_ptr(), a.val.dtype, args.algo, args.prec)
+        c = Cm.c
+        nt, nz = c.numtileC, c.nnzC
+        if out.get("nt") != nt or out.get("nz") != nz:
+            out.update(nt=nt, nz=nz, tp=pin(np.zeros(c.tilem + 1, np.int32)), r=pin(np.zeros(max(nt, 1), np.int32)),
+                       c=pin(np.zeros(max(nt, 1), np.int32)), p=pin(np.zeros(nt + 1, np.int64)),
+                       v=pin(np.zeros(max(nz, 1), np.float32)), cc=pin(np.zeros(max(nz, 1), np.uint8)))
+        g = lambda k: C.c_void_p(out[k].data_ptr())
+        h.check(h.lib.spg_ctiles_to_host(h.h, C.byref(c), g("tp"), g("r"), g("c"), None, g("p"), None, g("v"),
+                                         g("cc")))
+        Cm.free()
+        return (c.tilem + 1) * 4 + nt * 8 + (nt + 1) * 8 + nz * 5
+
+    try:
+        one()
+        torch.cuda.synchronize()
+        steps = max(1, args.e2e_steps)
+        t0 = time.perf_counter()
+        d2h = 0
+        for _ in range(steps):
+            d2h = one()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": dt * 1e3, "steps": steps,
+                "path": "pinned host CSR A and P -> device, spg_galerkin, spg_ctiles_to_host of tile_ptrC, "
+                        "tile_rowidxC, tile_colidxC, tile_nnzC, tile_valC, tile_colC to pinned host memory"}
+    except Exception as e:  # report instead of dying
+        return {"value": None, "unit": "GFLOP/s", "error": str(e)[:200], "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": None}
 
 
 def measure_e2e(h, api, a, b, args, flops, stream):
@@ -600,7 +963,9 @@ def run_batch(args):
     thr, algos = bt.tune()
     clocks = ClockSampler(local)
     clocks.start()
+    l0 = h.launches()
     ms_batch = timed(lambda: bt.spgemm(), args.steps)
+    launches = (h.launches() - l0) * args.steps // (args.steps + args.warmup)
     clk = clocks.stop()
     # (3) numeric-only graph replay with new values (same structure)
     nz = bt.bins()
@@ -617,15 +982,16 @@ def run_batch(args):
             "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "float32", "data": "synthetic",
             "config": {"workload": f"batch of {count} C=A*B, n log-uniform [1024,65536], Erdos-Renyi deg U[4,32], "
-                                   "FP32 U[-1,1]", "products": flops / 2, "tuned_thresholds": thr,
-                       "tuned_algos": algos, "plain_launches_ms": ms_plain,
-                       "plain_launches_gflops": flops / (ms_plain * 1e-3) / 1e9,
-                       "graph_numeric_ms": ms_graph, "graph_numeric_gflops": flops / (ms_graph * 1e-3) / 1e9,
-                       "speedup_batched_vs_plain_launches": ms_plain / ms_batch},
+                                   "FP32 U[-1,1]", "products": flops / 2},
+            "details": {"tuned_thresholds": thr, "tuned_algos": algos,
+                        "graph_numeric_ms": ms_graph, "graph_numeric_gflops": flops / (ms_graph * 1e-3) / 1e9},
+            "vs_plain": {"plain": {"ms_step": ms_plain, "gflops": flops / (ms_plain * 1e-3) / 1e9,
+                                   "what": "one plain launch sequence per product"},
+                         "speedup_vs_plain": ms_plain / ms_batch},
             "e2e": {"value": flops / (ms_graph * 1e-3) / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "path": "CUDA graph: new values host->device, numeric, C values "
                                                        "device->host (structure fixed)"},
-            "clocks": clk}
+            "clocks": clk, "gpu_launches": launches}
     if rank == 0:
         print(json.dumps(line), flush=True)
     bt.free()
@@ -643,6 +1009,10 @@ def main():
     p.add_argument("--prec", default="f32", choices=["f32", "mixed", "f64"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-check", action="store_true", help="skip the FP64-oracle check of C (on by default)")
+    p.add_argument("--no-compare", action="store_true",
+                   help="skip timing the plain kernels and the path without the sizing model (on by default)")
+    p.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain-kernel comparison")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--e2e-bands", type=int, default=8,
                    help="tile-row bands of the e2e numeric phase (a band's values copy once it is complete)")
@@ -655,7 +1025,6 @@ def main():
     p.add_argument("--cpu-s", type=float, default=12.0)
     p.add_argument("--ref-step-s", type=float, default=8.0)
     p.add_argument("--batch-count", type=int, default=512)
-    p.add_argument("--check", action="store_true", help="value error vs the FP64 oracle on a prefix of C")
     p.add_argument("--sizing", type=int, default=1, help="attach the trained sizing MLP (1) or not (0)")
     p.add_argument("--sizing-margin", type=float, default=1.0,
                    help="slot of a tile-row = predicted tiles * (1 + margin) + 2")

@@ -274,15 +274,55 @@ def products(a: CSR, b: CSR) -> int:
     return int(blen[a.col_idx].sum())
 
 
-def load_mtx(path: str, dtype=np.float64) -> CSR:
-    """Matrix Market reader following src/tile_format.h:51-90 (symmetric entries
-    expanded, pattern values 1.0, real part of complex values, sorted by (row, col)),
-    with duplicate entries summed."""
-    import scipy.io
-    import scipy.sparse as sp
-    M = scipy.io.mmread(path)
-    if not sp.issparse(M):
-        M = sp.csr_matrix(M)
-    if np.iscomplexobj(M.data):
-        M = M.real
-    return CSR.from_scipy(sp.csr_matrix(M, dtype=np.float64), dtype=dtype)
+def read_mtx_entries(path: str):
+    """Matrix Market coordinate file -> (m, n, rows, cols, vals) the way the
+    reference reads it (src/tile_format.h:51-90): the banner line's words
+    "symmetric", "pattern" and "complex" set the mode (so a skew-symmetric
+    file is mirrored like a symmetric one, with the same value), '%' lines
+    are skipped, indices are 1-based, pattern entries are 1.0, complex
+    entries keep their real part, and every off-diagonal entry of a
+    symmetric file is mirrored.  Entries come back in file order."""
+    with open(path) as f:
+        banner = f.readline()
+        sym, pat, cplx = "symmetric" in banner, "pattern" in banner, "complex" in banner
+        line = f.readline()
+        while line and line.startswith("%"):
+            line = f.readline()
+        m, n, nf = (int(x) for x in line.split()[:3])
+        per = 2 if pat else (4 if cplx else 3)
+        data = np.array(f.read().split()[:nf * per], dtype=np.float64).reshape(nf, per) if nf else \
+            np.zeros((0, per))
+    rows = data[:, 0].astype(np.int64) - 1
+    cols = data[:, 1].astype(np.int64) - 1
+    vals = np.ones(nf) if pat else data[:, 2].copy()
+    if sym:
+        off = rows != cols
+        # the mirrored entry follows its original, as the reader pushes them
+        rows = np.stack([rows, np.where(off, cols, -1)], 1).ravel()
+        cols = np.stack([cols, np.where(off, data[:, 0].astype(np.int64) - 1, -1)], 1).ravel()
+        vals = np.stack([vals, vals], 1).ravel()
+        keep = rows >= 0
+        rows, cols, vals = rows[keep], cols[keep], vals[keep]
+    return m, n, rows, cols, vals
+
+
+def load_mtx(path: str, dtype=np.float64, merge: bool = True) -> CSR:
+    """Matrix Market reader following src/tile_format.h:51-90 (see
+    read_mtx_entries), rows sorted by (row, col).  merge=True (the default)
+    also sums duplicate entries, which the reference keeps: the library
+    wants canonical CSR, columns strictly ascending inside each row.  With
+    merge=False duplicates stay, in file order, as the reference's CSR holds
+    them (its sort leaves their order unspecified)."""
+    m, n, rows, cols, vals = read_mtx_entries(path)
+    order = np.lexsort((cols, rows))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    if merge and rows.size:
+        key = rows * max(n, 1) + cols
+        first = np.concatenate([[True], key[1:] != key[:-1]])
+        seg = np.cumsum(first) - 1
+        vals = np.bincount(seg, weights=vals, minlength=int(seg[-1]) + 1)
+        rows, cols = rows[first], cols[first]
+    counts = np.bincount(rows, minlength=m).astype(np.int64)
+    rp = np.zeros(m + 1, np.int64)
+    np.cumsum(counts, out=rp[1:])
+    return CSR(m, n, rp.astype(np.int32), cols.astype(np.int32), np.ascontiguousarray(vals.astype(dtype)))

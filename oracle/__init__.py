@@ -59,6 +59,8 @@ def _declare(l):
         "orc_gustavson_fill_f32": (None, [I, I, P, P, P, P, P, P, P, P, P]),
         "orc_gustavson_range_f64": (L, [I, I, I, P, P, P, P, P, P, P]),
         "orc_gustavson_range_f32": (L, [I, I, I, P, P, P, P, P, P, P]),
+        "orc_check_tilerows_f64": (None, [I, I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
+        "orc_check_tilerows_f32": (None, [I, I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
         "orc_max_threads": (I, []),
         "orc_set_threads": (None, [I]),
     }
@@ -224,6 +226,33 @@ def gustavson_rows(a, b, r0: int, r1: int, dtype=np.float32) -> int:
     rn = np.zeros(max(r1 - r0, 1), np.int64)
     f = l.orc_gustavson_range_f64 if dtype == np.float64 else l.orc_gustavson_range_f32
     return int(f(r0, r1, b.n, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(rn)))
+
+
+def check_tilerows(a, b, i0: int, i1: int, tiles: dict) -> dict:
+    """Compare C tile-rows [i0, i1) of A*B given as tiles (keys ``tile_ptr``:
+    i1-i0+1 tile offsets from 0, ``tile_colidxC``, ``tile_nnzC``: absolute
+    nonzero prefix of those tiles, ``maskC``, ``ptrRowC``, ``tile_colC``,
+    ``tile_valC`` starting at the first tile's first value) with the FP64
+    Gustavson of the same rows (src/spgemm_raw_v2.cu:289-338).  Returns the
+    relative Frobenius error and the count of structural mismatches."""
+    l = lib()
+    vt = np.float64 if np.dtype(tiles["tile_valC"].dtype) == np.float64 else np.float32
+    arp, aci, brp, bci = _i32(a.row_ptr), _i32(a.col_idx), _i32(b.row_ptr), _i32(b.col_idx)
+    av = np.ascontiguousarray(a.val, vt)
+    bv = np.ascontiguousarray(b.val, vt)
+    ctp = np.ascontiguousarray(tiles["tile_ptr"], np.int64)
+    ccol = _i32(tiles["tile_colidxC"])
+    cnz = np.ascontiguousarray(tiles["tile_nnzC"], np.int64)
+    cmask = np.ascontiguousarray(tiles["maskC"], np.uint16)
+    cptr = np.ascontiguousarray(tiles["ptrRowC"], np.uint8)
+    ccolb = np.ascontiguousarray(tiles["tile_colC"], np.uint8)
+    cval = np.ascontiguousarray(tiles["tile_valC"], vt)
+    out = np.zeros(3, np.float64)
+    f = l.orc_check_tilerows_f64 if vt == np.float64 else l.orc_check_tilerows_f32
+    f(int(i0), int(i1), int(a.m), int(b.n), _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(ctp), _p(ccol),
+      _p(cnz), _p(cmask), _p(cptr), _p(ccolb), _p(cval), _p(out))
+    return {"rel_frob": float(np.sqrt(out[0]) / (np.sqrt(out[1]) or 1.0)), "mismatches": int(out[2]),
+            "ref_frob": float(np.sqrt(out[1]))}
 
 
 def max_threads() -> int:

@@ -4,9 +4,11 @@
 # oracle/_ref/ref_kernels.cubin from its kernel headers.
 # TEST INFRASTRUCTURE: used only to pin the oracle and to write the golden
 # fixtures under tests/golden/.  Skipped when the reference is absent.
+# The checkout is the first argument, else $SPG_REFERENCE_DIR, else a
+# "reference" directory beside this repository.
 set -e
-REF=${SPG_REFERENCE_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${SPG_REFERENCE_DIR:-$HERE/../../reference}}
 if [ ! -f "$REF/src/tile_format.h" ]; then
   echo "reference not found at $REF; skipping oracle/_ref" >&2
   exit 0

@@ -57,3 +57,20 @@ def ref_tiles(csr, csc: bool) -> dict:
               *(g(k).ctypes.data if g(k) is not None else z for k in
                 ("csc_tile_ptr", "csc_tile_rowidx", "tile_csc_Ptr", "tile_csc_Row", "tile_csc_Val")))
     return o
+
+
+def ref_load_mtx(path: str):
+    """The reference's load_mtx (src/tile_format.h:51-90) on a file: returns
+    (m, n, row_ptr, col_idx, val) with duplicates kept."""
+    l = C.CDLL(LIB)
+    l.ref_mtx_load.restype = C.c_int
+    l.ref_mtx_load.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    l.ref_mtx_get.restype = None
+    l.ref_mtx_get.argtypes = [C.c_void_p] * 3
+    m, n, nz = C.c_int(), C.c_int(), C.c_int()
+    l.ref_mtx_load(path.encode(), C.byref(m), C.byref(n), C.byref(nz))
+    rp = np.zeros(m.value + 1, np.int32)
+    ci = np.zeros(nz.value, np.int32)
+    val = np.zeros(nz.value, np.float64)
+    l.ref_mtx_get(rp.ctypes.data, ci.ctypes.data, val.ctypes.data)
+    return m.value, n.value, rp, ci, val

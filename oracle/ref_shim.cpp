@@ -45,3 +45,22 @@ extern "C" void ref_get(int* tile_ptr, int* tile_columnidx, int* tile_nnz, unsig
         memcpy(tcsc_val, T.tile_csc_Val, sizeof(double) * nz);
     }
 }
+
+// The reference's own Matrix Market reader (src/tile_format.h:51-90): loads
+// `path` and gives m, n and the entry count; ref_mtx_get copies the
+// CSR it built (duplicates kept, as the reference keeps them).
+static HostCSR g_mtx;
+
+extern "C" int ref_mtx_load(const char* path, int* m, int* n, int* nnz) {
+    g_mtx = load_mtx(path);
+    *m = g_mtx.m;
+    *n = g_mtx.n;
+    *nnz = g_mtx.nnz;
+    return 0;
+}
+
+extern "C" void ref_mtx_get(int* rp, int* ci, double* val) {
+    memcpy(rp, g_mtx.row_ptr.data(), sizeof(int) * (g_mtx.m + 1));
+    memcpy(ci, g_mtx.col_idx.data(), sizeof(int) * g_mtx.nnz);
+    for (int i = 0; i < g_mtx.nnz; i++) val[i] = (double)g_mtx.val[i];
+}

@@ -14,6 +14,8 @@
  *   orc_step3_numeric                  src/spgemm_raw_kernels_v2.cuh:10-139
  *   orc_tiles_to_csr                   src/spgemm_raw_v2.cu:268-284
  *   orc_gustavson_*                    src/spgemm_raw_v2.cu:289-338
+ *   orc_check_tilerows_*               the same Gustavson, compared with C tiles
+ *                                      laid out as src/spgemm_raw_kernels_v2.cuh:120-136
  * Values are carried in double; the tile format arrays are bit-identical to the
  * reference's for inputs in canonical CSR form (columns strictly ascending).
  */
@@ -514,6 +516,85 @@ GUSTAVSON_FILL(orc_gustavson_fill_f32, float)
 
 GUSTAVSON_RANGE(orc_gustavson_range_f64, double)
 GUSTAVSON_RANGE(orc_gustavson_range_f32, float)
+
+/* ------------------------------------------------------------------------ */
+/* Checker of C tile-rows [i0, i1) produced elsewhere (the GPU library):     */
+/* every row of those tile-rows is formed by the FP64 Gustavson above        */
+/* (src/spgemm_raw_v2.cu:289-338, products in double) and compared entry by  */
+/* entry with the given tiles, read the way steps 1-3 lay them out           */
+/* (src/spgemm_raw_kernels_v2.cuh:120-136: a row's entries sit at            */
+/* tile_nnzC[t] + ptrRowC[t][r], one per set bit of maskC[t][r], MSB first,  */
+/* column byte (r<<4)|c).  Tile-row i's tiles are [ctp[i-i0], ctp[i-i0+1])   */
+/* of the arrays; cnz holds their absolute nonzero prefix, values and column */
+/* bytes start at cnz[0].  out[0] = sum of squared differences, out[1] = sum */
+/* of squared FP64 values, out[2] = structural mismatches (an entry in one   */
+/* and not the other, a column byte that disagrees with the mask, a tile     */
+/* count that disagrees with its masks).  OpenMP over rows.                  */
+/* ------------------------------------------------------------------------ */
+#define CHECK_TILEROWS(NAME, T)                                                              \
+    void NAME(int i0, int i1, int m, int n, const int* arp, const int* aci, const T* av,      \
+              const int* brp, const int* bci, const T* bv, const int64_t* ctp, const int* ccol, \
+              const int64_t* cnz, const uint16_t* cmask, const uint8_t* cptr,                 \
+              const uint8_t* ccolb, const T* cval, double* out) {                             \
+        double err = 0.0, ref = 0.0;                                                          \
+        int64_t bad = 0;                                                                      \
+        const int r0 = i0 * TS;                                                               \
+        for (int64_t t = ctp[0]; t < ctp[i1 - i0]; t++) {                                     \
+            int64_t pc = 0;                                                                   \
+            for (int r = 0; r < TS; r++) pc += __builtin_popcount(cmask[t * TS + r]);         \
+            if (pc != cnz[t + 1] - cnz[t]) bad++;                                             \
+        }                                                                                     \
+        _Pragma("omp parallel reduction(+ : err, ref, bad)") {                                \
+            double* acc = (double*)calloc((size_t)n + 1, sizeof(double));                     \
+            char* used = (char*)calloc((size_t)n + 1, 1);                                     \
+            int* cols = (int*)malloc(sizeof(int) * ((size_t)n + 1));                          \
+            _Pragma("omp for schedule(dynamic, 16)") for (int r = r0; r < i1 * TS; r++) {     \
+                const int i = r / TS, lr = r % TS;                                            \
+                int nc = 0;                                                                   \
+                if (r < m)                                                                    \
+                    for (int ja = arp[r]; ja < arp[r + 1]; ja++) {                            \
+                        const int k = aci[ja];                                                \
+                        const double va = (double)av[ja];                                     \
+                        for (int jb = brp[k]; jb < brp[k + 1]; jb++) {                        \
+                            const int c = bci[jb];                                            \
+                            if (!used[c]) { used[c] = 1; cols[nc++] = c; }                    \
+                            acc[c] += va * (double)bv[jb];                                    \
+                        }                                                                     \
+                    }                                                                         \
+                for (int64_t t = ctp[i - i0]; t < ctp[i - i0 + 1]; t++) {                     \
+                    const unsigned m16 = cmask[t * TS + lr];                                  \
+                    int64_t e = cnz[t] - cnz[0] + cptr[t * TS + lr];                          \
+                    for (int b = 0; b < TS; b++) {                                            \
+                        if (!(m16 & (0x8000u >> b))) continue;                                \
+                        const int c = ccol[t] * TS + b;                                       \
+                        if (ccolb[e] != (uint8_t)((lr << 4) | b) || c >= n || r >= m ||       \
+                            used[c] != 1) {                                                   \
+                            bad++;                                                            \
+                        } else {                                                              \
+                            const double d = (double)cval[e] - acc[c];                        \
+                            err += d * d;                                                     \
+                            used[c] = 2;                                                      \
+                        }                                                                     \
+                        e++;                                                                  \
+                    }                                                                         \
+                }                                                                             \
+                for (int q = 0; q < nc; q++) {                                                \
+                    const int c = cols[q];                                                    \
+                    if (used[c] != 2) bad++;                                                  \
+                    ref += acc[c] * acc[c];                                                   \
+                    acc[c] = 0.0;                                                             \
+                    used[c] = 0;                                                              \
+                }                                                                             \
+            }                                                                                 \
+            free(acc); free(used); free(cols);                                                \
+        }                                                                                     \
+        out[0] = err;                                                                         \
+        out[1] = ref;                                                                         \
+        out[2] = (double)bad;                                                                 \
+    }
+
+CHECK_TILEROWS(orc_check_tilerows_f64, double)
+CHECK_TILEROWS(orc_check_tilerows_f32, float)
 
 int orc_max_threads(void) {
 #ifdef _OPENMP

@@ -145,3 +145,31 @@ def test_oracle_c_structure_matches_reference_kernels(path):
     ref = z["tile_valC"]
     den = np.linalg.norm(ref) or 1.0
     assert np.linalg.norm(S["tile_valC"] - ref) / den <= 1e-12
+
+
+@pytest.mark.parametrize("name,a,b", cases.product_cases(), ids=[c[0] for c in cases.product_cases()])
+def test_tilerow_checker_accepts_the_oracle_and_catches_planted_errors(name, a, b):
+    """oracle.check_tilerows (the FP64 row Gustavson compared entry by entry
+    with C's tiles, used on the full-size GPU products) reports no error on
+    the tiled oracle's own C, and catches a value and a mask bit changed in
+    a copy of it."""
+    S = oracle.spgemm_tiles(a, b)
+    tilem = S["tilem"]
+    tp = S["tile_ptrC"].astype(np.int64)
+    for i0, i1 in ((0, tilem), (tilem // 3, tilem)):
+        t0, t1 = tp[i0], tp[i1]
+        v0, v1 = S["tile_nnzC"][t0], S["tile_nnzC"][t1]
+        d = dict(tile_ptr=tp[i0:i1 + 1] - t0, tile_colidxC=S["tile_colidxC"][t0:t1], tile_nnzC=S["tile_nnzC"][t0:t1 + 1],
+                 maskC=S["maskC"][t0 * 16:t1 * 16], ptrRowC=S["ptrRowC"][t0 * 16:t1 * 16],
+                 tile_colC=S["tile_colC"][v0:v1], tile_valC=S["tile_valC"][v0:v1])
+        r = oracle.check_tilerows(a, b, i0, i1, d)
+        assert r["mismatches"] == 0 and r["rel_frob"] <= 1e-14, r
+        if v1 > v0:
+            bad = dict(d, tile_valC=d["tile_valC"].copy())
+            bad["tile_valC"][(v1 - v0) // 2] += 1.0
+            assert oracle.check_tilerows(a, b, i0, i1, bad)["rel_frob"] > 0
+            bad = dict(d, maskC=d["maskC"].copy())
+            k = int(np.flatnonzero(bad["maskC"])[0])
+            mk = int(bad["maskC"][k])
+            bad["maskC"][k] = np.uint16(mk & (mk - 1))  # one entry dropped from the mask
+            assert oracle.check_tilerows(a, b, i0, i1, bad)["mismatches"] > 0

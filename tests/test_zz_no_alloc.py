@@ -63,6 +63,38 @@ def test_noalloc_export_matches_allocating_export_twice(h):
     assert grabbed[1] == 0
 
 
+def test_noalloc_export_fp64_twice(h):
+    """FP64 values take the double fill; again a larger C, then a smaller one."""
+    for a in (synth.poisson2d(64), synth.rmat(11, 16, dtype=np.float64)):
+        A = api.csr2tile(h, a)
+        B = api.build_csc_tiles(h, a)
+        Cm = api.spgemm(h, A, B)
+        rp0, ci0, v0 = api.ctiles_to_csr(h, Cm)
+        rp1, ci1, v1, _ = _export_noalloc(h, Cm)
+        assert v1.dtype == np.float64
+        np.testing.assert_array_equal(rp1, rp0)
+        np.testing.assert_array_equal(ci1, ci0)
+        np.testing.assert_array_equal(v1, v0)
+
+
+@pytest.mark.parametrize("m,n", [(0, 16), (40, 24)], ids=["no-rows", "rows-without-nonzeros"])
+def test_noalloc_export_of_an_empty_c(h, m, n):
+    """A C with no rows, and a C whose rows hold nothing: the row pointer is
+    all zeros (m+1 entries), nothing else is written, nnz is 0."""
+    a = synth.CSR(m, n, np.zeros(m + 1, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32))
+    rng = np.random.Generator(np.random.PCG64(3))
+    b = synth.erdos_renyi(n, 4.0, rng)  # B has entries; A reaches none of them
+    A = api.csr2tile(h, a)
+    B = api.build_csc_tiles(h, b)
+    Cm = api.spgemm(h, A, B)
+    assert Cm.nnzC == 0
+    rp0, _, _ = api.ctiles_to_csr(h, Cm)
+    rp1, ci1, v1, _ = _export_noalloc(h, Cm)
+    np.testing.assert_array_equal(rp1, np.zeros(m + 1, np.int32))
+    np.testing.assert_array_equal(rp1, rp0)
+    assert ci1.size == 0 and v1.size == 0
+
+
 def test_noalloc_rejects_more_rows_than_its_area(h):
     m = MAX_ROWS + 16
     a = synth.CSR(m, 16, np.zeros(m + 1, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32))
