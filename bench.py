@@ -54,6 +54,10 @@ TS = 16
 # traffic is this ratio times its algorithmic bytes.
 TRAFFIC_PER_ALGO_BYTE = {"rw_numeric_kernel": None}
 
+# A tiles from which the bench attaches the learned sizing model (step 1's
+# slotted pass); the library's AUTO bins tile-rows from the same size on.
+SIZING_MIN_TILES = 65536
+
 
 # ---------------------------------------------------------------------------
 # workloads
@@ -70,6 +74,10 @@ def workload(name: str) -> dict:
     if name == "stencil27":
         a = synth.stencil27_dof3(64)
         return dict(kind="product", a=a, b=a, desc="C=A*A, A=27-point stencil 64^3 x 3 dof, FP32 N(0,1)")
+    if name == "mixed":
+        a = synth.block_diag(synth.stencil27_dof3(40), synth.rmat(18, 16))
+        return dict(kind="product", a=a, b=a, desc="C=A*A, A=block diagonal of a 27-point stencil 40^3 x 3 dof "
+                                                   "(FP32 N(0,1)) and R-MAT scale 18, edge factor 16")
     if name.startswith("galerkin"):
         g = int(name[8:] or 128)
         a = synth.poisson3d(g)
@@ -451,7 +459,10 @@ def run_ours(args):
     flops = 2.0 * products
     h.set_mixed_params(args.dense_thr)
     sizing = None
-    if args.sizing and os.path.exists(api.SIZING_MODEL_PATH):
+    # the learned step 1 pays three read-backs where the exact one pays one:
+    # it is attached for an A of at least 65,536 tiles, where its single
+    # bitmap pass saves more than they cost
+    if args.sizing and os.path.exists(api.SIZING_MODEL_PATH) and A.numtile >= SIZING_MIN_TILES:
         sizing = api.SizingModel.load(h)
         sizing.attach(args.sizing_margin)
     timer = Timer(stream, needs_flush(w))
@@ -486,7 +497,7 @@ def run_ours(args):
     s1 = statistics.mean(s["ms_step1"] for s in stats)
     s2 = statistics.mean(s["ms_step2"] for s in stats)
     s3 = statistics.mean(s["ms_step3"] for s in stats)
-    rowwise = stats[-1].get("algo_used", 1) == 2
+    rowwise = stats[-1].get("algo_used", 1) in (2, 3)
     roofline, ab_bytes = step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sizing is not None)
     c_b = c_bytes(numtileC, nnzC, A.tilem, v)
 
@@ -537,12 +548,13 @@ def run_ours(args):
         hbm_peak = roofline["peak"]
         hbm_steps = (ab_bytes + c_b) / (ms * 1e-3) / 1e9
         details = {"numtileC": numtileC, "nnzC": nnzC, "tile_pairs": pairs, "algo": args.algo, "prec": args.prec,
-                   "algo_used": {0: "auto", 1: "plain", 2: "rowwise"}.get(stats[-1].get("algo_used"), "?"),
+                   "algo_used": {0: "auto", 1: "plain", 2: "rowwise", 3: "binned"}.get(stats[-1].get("algo_used"), "?"),
                    "ms_step1": s1, "ms_step2": s2, "ms_step3": s3,
                    "tile_bytes": {"A+B": ab_bytes, "C": c_b},
                    "hbm_gbs_steps": hbm_steps, "hbm_frac_steps": hbm_steps / hbm_peak,
                    "tensor_pairs": stats[-1].get("tensor_pairs", 0), "fp64_tiles": stats[-1].get("fp64_tiles", 0),
-                   "learned_sizing": None if sizing is None else {
+                   "learned_sizing": "not attached: A has fewer than %d tiles" % SIZING_MIN_TILES
+                   if sizing is None and args.sizing else None if sizing is None else {
                        "model": os.path.relpath(api.SIZING_MODEL_PATH, ROOT), "margin": args.sizing_margin,
                        "predicted_tiles": stats[-1].get("predicted_tiles", 0), "actual_tiles": numtileC,
                        "overflow_reruns": stats[-1].get("overflow_reruns", 0),
@@ -663,7 +675,8 @@ def run_galerkin(args, w, world, rank, local):
                    "ms_steps_of_both_products": {"step1": st["ms_step1"], "step2": st["ms_step2"],
                                                  "step3": st["ms_step3"]},
                    "ms_tiling_and_conversions": ms_local - s123,
-                   "learned_sizing": None if sizing is None else {"margin": args.sizing_margin,
+                   "learned_sizing": "not attached: A has fewer than %d tiles" % SIZING_MIN_TILES
+                   if sizing is None and args.sizing else None if sizing is None else {"margin": args.sizing_margin,
                                                                   "overflow_reruns": st["overflow_reruns"]}}
         steps_ms = {"step1": st["ms_step1"], "step2": st["ms_step2"], "step3": st["ms_step3"],
                     "tiling and conversions": ms_local - s123}
@@ -1005,7 +1018,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="rmat20")
-    p.add_argument("--algo", default="auto", choices=["auto", "plain", "rowwise"])
+    p.add_argument("--algo", default="auto", choices=["auto", "plain", "rowwise", "binned"])
     p.add_argument("--prec", default="f32", choices=["f32", "mixed", "f64"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")

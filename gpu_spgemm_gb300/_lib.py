@@ -19,7 +19,7 @@ SPG_F32, SPG_F64 = 0, 1
 SPG_LAYOUT_ROW, SPG_LAYOUT_B_CSC = 0, 1
 SPG_TILE_WITH_TILE_CSC = 1
 SPG_TILE = 16  # tile edge
-SPG_ALGO_AUTO, SPG_ALGO_PLAIN, SPG_ALGO_ROWWISE = 0, 1, 2
+SPG_ALGO_AUTO, SPG_ALGO_PLAIN, SPG_ALGO_ROWWISE, SPG_ALGO_BINNED = 0, 1, 2, 3
 SPG_PREC_F32, SPG_PREC_MIXED, SPG_PREC_F64 = 0, 1, 2
 SPG_BANDS_FIRST_TO_LAST, SPG_BANDS_LAST_TO_FIRST = 0, 1
 
@@ -100,6 +100,7 @@ SIGNATURES = {
     "spg_mlp_train": (I32, [P, P, P, P, I64, P, I32, I32, C.c_float, P]),
     "spg_set_sizing_model": (I32, [P, P, C.c_float]),
     "spg_set_mixed_params": (I32, [P, C.c_int, C.c_float]),
+    "spg_set_bin_params": (I32, [P, C.c_float, C.c_float]),
     "spg_symbolic_tiles": (I32, [P, P, P, C.c_int, P]),
     "spg_symbolic_masks": (I32, [P, P, P, P]),
     "spg_numeric_rows": (I32, [P, P, P, I32, I32, P, I32, I32]),

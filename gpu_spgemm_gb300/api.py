@@ -18,7 +18,8 @@ import numpy as np
 from . import _lib as L
 
 TS = 16
-_ALGOS = {"auto": L.SPG_ALGO_AUTO, "plain": L.SPG_ALGO_PLAIN, "rowwise": L.SPG_ALGO_ROWWISE}
+_ALGOS = {"auto": L.SPG_ALGO_AUTO, "plain": L.SPG_ALGO_PLAIN, "rowwise": L.SPG_ALGO_ROWWISE,
+          "binned": L.SPG_ALGO_BINNED}
 _PRECS = {"f32": L.SPG_PREC_F32, "mixed": L.SPG_PREC_MIXED, "f64": L.SPG_PREC_F64}
 
 
@@ -62,6 +63,12 @@ class Handle:
         """SPG_PREC_MIXED: tensor-core threshold (nonzeros in both tiles) and
         the cancellation bound that sends a C tile to FP64."""
         self.check(self.lib.spg_set_mixed_params(self.h, int(dense_thr), float(cancel_eps)))
+
+    def set_bin_params(self, pp_thr: float = 12.0, fill_thr: float = 16.0):
+        """SPG_ALGO_BINNED / AUTO: a tile-row runs the plain kernels when its
+        products per tile pair reach pp_thr and (with a sizing model) its
+        predicted C nonzeros per C tile reach fill_thr."""
+        self.check(self.lib.spg_set_bin_params(self.h, float(pp_thr), float(fill_thr)))
 
     def stats(self) -> dict:
         st = L.SpgStats()

@@ -244,6 +244,29 @@ __global__ void mlp_slot_kernel(int tilem, int tilenB, const float* __restrict__
     }
 }
 
+// Kernel variant of each C tile-row (1: the plain per-C-tile kernels, 0: the
+// row-wise windows).  The plain kernels spend one warp pass of 16x16 register
+// accumulators per matched tile pair and write every C tile whole, so they
+// pay off where a tile pair carries many products and C's tiles come out
+// full; the row-wise windows spend their time per product.  A tile-row goes
+// to the plain kernels when its products per tile pair (features 3 and 2,
+// exact) reach pp_thr and, with a sizing model, its predicted C nonzeros per
+// predicted C tile (the network's two outputs) reach fill_thr.
+__global__ void bin_rows_kernel(int tilem, const float* __restrict__ feat, const float* __restrict__ pred,
+                                float pp_thr, float fill_thr, uint8_t* __restrict__ bin) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
+        const float* f = feat + (int64_t)i * NF;
+        const float pairs = expm1f(f[2]), prod = expm1f(f[3]);
+        bool plain = pairs > 0.5f && prod >= pp_thr * pairs;
+        if (plain && pred) {
+            const float tiles = expm1f(fmaxf(pred[(int64_t)i * NO + 0], 0.f));
+            const float nnz = expm1f(fmaxf(pred[(int64_t)i * NO + 1], 0.f));
+            plain = nnz >= fill_thr * fmaxf(tiles, 1.f);
+        }
+        bin[i] = plain ? 1 : 0;
+    }
+}
+
 int mgrid(spg_handle_t h, int64_t n, int threads) {
     int64_t g = ceil_div(n, threads);
     if (g > (int64_t)h->num_sms * 8) g = (int64_t)h->num_sms * 8;
@@ -399,18 +422,25 @@ extern "C" spg_status spg_set_sizing_model(spg_handle_t h, spg_mlp_t mm, float m
 }
 
 // Predicted capacities for C of A*B (tiles, nonzeros) from the sizing model.
-spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz) {
+spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz, uint8_t* rowbin) {
     spg_mlp_t mm = h->sizing;
     const int tilem = A->tilem;
     ScratchList sc(h);
     float *feat = nullptr, *pred = nullptr;
     SPG_TRY(sc.alloc(&feat, (size_t)tilem * NF + 1));
-    SPG_TRY(sc.alloc(&pred, (size_t)tilem * NO + 1));
     SPG_TRY(spg_mlp_features(h, A, B, feat));
-    SPG_TRY(spg_mlp_forward(h, mm, feat, tilem, pred));
-    if (tilem > 0) {
+    if (mm) {
+        SPG_TRY(sc.alloc(&pred, (size_t)tilem * NO + 1));
+        SPG_TRY(spg_mlp_forward(h, mm, feat, tilem, pred));
+    }
+    if (tilem > 0 && slot_sz && mm) {
         mlp_slot_kernel<<<mgrid(h, tilem, 256), 256, 0, h->stream>>>(tilem, B->tilen, feat, pred, h->sizing_margin,
                                                                    slot_sz);
+        SPG_LAUNCHED(h);
+    }
+    if (tilem > 0 && rowbin) {
+        bin_rows_kernel<<<mgrid(h, tilem, 256), 256, 0, h->stream>>>(tilem, feat, pred, h->bin_pp_thr,
+                                                                   h->bin_fill_thr, rowbin);
         SPG_LAUNCHED(h);
     }
     return SPG_OK;

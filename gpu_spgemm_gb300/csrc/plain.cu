@@ -213,14 +213,15 @@ __device__ __forceinline__ int lower_bound_dev(const int* __restrict__ a, int lo
 // each pair ORs B's row masks selected by A's column bytes into C's 16 row
 // masks (:173-184); up to SPEC_MAX pairs are cached for step 3 with the bound
 // checked before any write (the reference writes past its buffer first).
-template <bool CACHE>
+template <bool CACHE, typename CNT = int, bool LIST = false>
 __global__ void __launch_bounds__(128)
-c2_symbolic_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
+c2_symbolic_kernel(int64_t ntiles, const int* __restrict__ tlist, const int* __restrict__ rowidxC,
+                   const int* __restrict__ colidxC,
                    const int* __restrict__ a_tp, const int* __restrict__ a_tc,
                    const int* __restrict__ a_tnnz, const uint8_t* __restrict__ a_col,
                    const uint8_t* __restrict__ a_ptr16, const int* __restrict__ b_cscp,
                    const int* __restrict__ b_cscr, const uint16_t* __restrict__ b_mask,
-                   uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC, int* __restrict__ tile_cnt,
+                   uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC, CNT* __restrict__ tile_cnt,
                    int* __restrict__ spec_cnt, int* __restrict__ spec_off, int* __restrict__ spec_pa,
                    int* __restrict__ spec_pb, int64_t spec_cap, unsigned long long* __restrict__ alloc_ctr,
                    unsigned long long* __restrict__ pairs_total, unsigned* flags) {
@@ -231,7 +232,8 @@ c2_symbolic_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int*
     const unsigned hmask = 0xffffu << (16 * half);
     unsigned long long my_pairs = 0;
     const int64_t nhw = (int64_t)gridDim.x * 8;
-    for (int64_t t = (int64_t)blockIdx.x * 8 + hw; t < numtileC; t += nhw) {
+    for (int64_t idx = (int64_t)blockIdx.x * 8 + hw; idx < ntiles; idx += nhw) {
+        const int64_t t = LIST ? (int64_t)tlist[idx] : idx;  // the C tile (a listed one, or every one)
         const int bi = rowidxC[t], bj = colidxC[t];
         const int as = a_tp[bi], ae = a_tp[bi + 1];
         const int bs = b_cscp[bj], be = b_cscp[bj + 1];
@@ -295,7 +297,7 @@ c2_symbolic_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int*
             if (r >= d) inc += o;
         }
         ptrRowC[t * TS + r] = (uint8_t)(inc - pc);
-        if (r == TS - 1) tile_cnt[t] = inc;
+        if (r == TS - 1) tile_cnt[t] = (CNT)inc;
     }
     my_pairs = warp_sum(my_pairs);
     if (lane == 0 && my_pairs) atomicAdd(pairs_total, my_pairs);
@@ -306,9 +308,10 @@ c2_symbolic_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int*
 // keep 16 register accumulators; B's row is walked through its 16-bit mask
 // with predicated FMAs instead of the reference's 16-way switch; a shuffle
 // combines the halves and half 0 compacts the row by maskC.
-template <typename V, bool CACHE, bool SKIP_DENSE = false>
+template <typename V, bool CACHE, bool SKIP_DENSE = false, bool LIST = false>
 __global__ void __launch_bounds__(256)
-c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* __restrict__ colidxC,
+c3_numeric_kernel(int64_t ntiles, const int* __restrict__ tlist, const int* __restrict__ rowidxC,
+                  const int* __restrict__ colidxC,
                   const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ a_tnnz,
                   const V* __restrict__ a_val, const uint8_t* __restrict__ a_col,
                   const uint8_t* __restrict__ a_ptr16, const int* __restrict__ b_cscp,
@@ -322,7 +325,8 @@ c3_numeric_kernel(int64_t numtileC, const int* __restrict__ rowidxC, const int* 
                   unsigned* __restrict__ n_dense_tiles = nullptr) {
     const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < numtileC; t += nwarps) {
+    for (int64_t idx = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < ntiles; idx += nwarps) {
+        const int64_t t = LIST ? (int64_t)tlist[idx] : idx;  // the C tile (a listed one, or every one)
         const int64_t cbase = tile_nnzC[t];
         if (tile_nnzC[t + 1] == cbase) continue;
         V acc[TS];
@@ -746,19 +750,17 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
     int64_t cap = 0;
     SPG_TRY(spg_read_i64(h, slot_off + tilem, &cap));
     h->stats.predicted_tiles = cap;
-    {   // the staging may take a quarter of the free device memory (C's arrays
-        // come after it); beyond that the caller runs the exact two passes
-        size_t fr = 0, tot = 0;
-        SPG_CUDA(h, cudaMemGetInfo(&fr, &tot));
-        unsigned long long budget = fr / 4;
-        if (const char* e = getenv("SPG_SLOT_BUDGET_BYTES")) budget = strtoull(e, nullptr, 10);
-        if ((unsigned long long)cap * sizeof(int) > budget)
-            return spg_fail(h, SPG_ERR_OOM, "step 1: predicted slots exceed the staging budget");
+    {   // an optional cap on the staging (SPG_SLOT_BUDGET_BYTES); without one
+        // the staging takes what the pool gives, and an allocation that fails
+        // sends the caller to the exact two passes, which need no staging
+        if (const char* e = getenv("SPG_SLOT_BUDGET_BYTES"))
+            if ((unsigned long long)cap * sizeof(int) > strtoull(e, nullptr, 10))
+                return spg_fail(h, SPG_ERR_OOM, "step 1: predicted slots exceed the staging budget");
     }
     int* slot_col = nullptr;
     int* cnt = nullptr;
     int64_t* ptr64 = nullptr;
-    SPG_TRY(sc.alloc(&slot_col, (size_t)cap + 1));
+    SPG_TRY(spg_workspace(h, SPG_WS_SLOTS, sizeof(int) * ((size_t)cap + 1), reinterpret_cast<void**>(&slot_col)));
     SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
     SPG_TRY(sc.alloc(&ptr64, (size_t)tilem + 1));
     if (tilem > 0) {
@@ -797,40 +799,56 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
     return SPG_OK;
 }
 
-spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                       PlainPriv* pp, int* tile_cnt) {
-    const int64_t nt = C->numtileC;
+// Step 2 over C's tiles, or over the listed ones (tlist: nlist ascending tile
+// indices); each tile's nonzero count goes to cnt32[t] or, when cnt32 is
+// null, to cnt64[t].
+template <typename CNT, bool LIST>
+static void launch_c2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
+                      int64_t nt, const int* tlist, CNT* cnt, int grid) {
+    unsigned long long* ctr = pp->counters;
+    if (pp->spec_cap > 0)
+        c2_symbolic_kernel<true, CNT, LIST><<<grid, 128, 0, h->stream>>>(
+            nt, tlist, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, cnt,
+            pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb, pp->spec_cap, ctr, ctr + 1, h->d_flags);
+    else
+        c2_symbolic_kernel<false, CNT, LIST><<<grid, 128, 0, h->stream>>>(
+            nt, tlist, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
+            A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, cnt,
+            nullptr, nullptr, nullptr, nullptr, 0, ctr, ctr + 1, h->d_flags);
+}
+
+spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
+                       int* cnt32, int64_t* cnt64, const int* tlist, int64_t nlist) {
+    const int64_t nt = tlist ? nlist : C->numtileC;
     unsigned long long* ctr = pp->counters;  // [0] alloc, [1] pairs
     SPG_CUDA(h, cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), h->stream));
     if (nt == 0) return SPG_OK;
     const int grid = grid_cap(h, nt, 8, 64);
     for (int attempt = 0; attempt < 2; attempt++) {
-        if (pp->spec_cap > 0) {
-            c2_symbolic_kernel<true><<<grid, 128, 0, h->stream>>>(
-                nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, A->tile_csr_Col,
-                A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, tile_cnt,
-                pp->spec_cnt, pp->spec_off, pp->spec_pa, pp->spec_pb, pp->spec_cap, ctr, ctr + 1, h->d_flags);
-        } else {
-            c2_symbolic_kernel<false><<<grid, 128, 0, h->stream>>>(
-                nt, C->tile_rowidxC, C->tile_colidxC, A->tile_ptr, A->tile_columnidx, A->tile_nnz, A->tile_csr_Col,
-                A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->mask, C->maskC, C->ptrRowC, tile_cnt,
-                nullptr, nullptr, nullptr, nullptr, 0, ctr, ctr + 1, h->d_flags);
-        }
+        if (cnt32 && !tlist)
+            launch_c2<int, false>(h, A, B, C, pp, nt, nullptr, cnt32, grid);
+        else if (cnt32)
+            launch_c2<int, true>(h, A, B, C, pp, nt, tlist, cnt32, grid);
+        else if (!tlist)
+            launch_c2<int64_t, false>(h, A, B, C, pp, nt, nullptr, cnt64, grid);
+        else
+            launch_c2<int64_t, true>(h, A, B, C, pp, nt, tlist, cnt64, grid);
         SPG_LAUNCHED(h);
         if (pp->spec_cap == 0) break;
         // overflow re-run (src/spgemm_raw_v2.cu:191-200, with the bound honoured in-kernel)
         int64_t used = 0;
-        SPG_TRY(spg_read_i64(h, (const int64_t*)ctr, &used));
-        unsigned fl = 0;
-        SPG_CUDA(h, cudaMemcpy(&fl, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
-        if (!(fl & DERR_OVERFLOW)) break;
-        SPG_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
+        const int64_t* src[1] = {(const int64_t*)ctr};
+        const spg_status rs = spg_read_i64s_checked(h, 1, src, &used, "symbolic step 2");
+        if (rs == SPG_OK) break;                      // no overflow
+        if (rs != SPG_ERR_OVERFLOW_RERUN) return rs;  // another device error
+        used = h->h_pinned[8];
         h->stats.overflow_reruns++;
         spg_free_async(h, pp->spec_pa);
         spg_free_async(h, pp->spec_pb);
         pp->spec_pa = pp->spec_pb = nullptr;
         size_t fr = 0, tot = 0;
-        cudaMemGetInfo(&fr, &tot);
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = 0;
         if (attempt == 0 && (size_t)used * 8 < fr / 2) {
             pp->spec_cap = used;
             SPG_TRY(spg_alloc_t(h, &pp->spec_pa, (size_t)used + 1));
@@ -866,32 +884,42 @@ static CTileView ctile_view(const spg_ctiles* C, const PlainPriv* pp, int64_t t0
 
 template <typename V>
 static spg_status plain_step3_t(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                                PlainPriv* pp, int64_t t0, int64_t t1) {
+                                PlainPriv* pp, int64_t t0, int64_t t1, const int* tlist) {
     const int64_t nt = t1 - t0;
     if (nt <= 0 || C->nnzC == 0) return SPG_OK;
-    const CTileView cv = ctile_view(C, pp, t0);
+    // a tile range is a view of C's arrays from t0; listed tiles index C whole
+    const CTileView cv = ctile_view(C, pp, tlist ? 0 : t0);
+    const int* lst = tlist ? tlist + t0 : nullptr;
     const int grid = grid_cap(h, nt, 8, 32);
-    if (pp && pp->spec_cap > 0)
-        c3_numeric_kernel<V, true><<<grid, 256, 0, h->stream>>>(
-            nt, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
-            (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
-            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,
-            (V*)C->tile_valC, C->tile_colC, cv.spec_cnt, cv.spec_off, pp->spec_pa, pp->spec_pb);
+    const bool cache = pp && pp->spec_cap > 0;
+#define C3_ARGS(SPEC)                                                                                              \
+    nt, lst, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const V*)A->tile_csr_Val,          \
+        A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz,                          \
+        (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16, (V*)C->tile_valC,            \
+        C->tile_colC, SPEC
+#define C3_SPEC cv.spec_cnt, cv.spec_off, pp->spec_pa, pp->spec_pb
+#define C3_NOSPEC nullptr, nullptr, nullptr, nullptr
+    // the list is a template flag: the whole-range kernel keeps its registers
+    if (cache && lst)
+        c3_numeric_kernel<V, true, false, true><<<grid, 256, 0, h->stream>>>(C3_ARGS(C3_SPEC));
+    else if (cache)
+        c3_numeric_kernel<V, true, false, false><<<grid, 256, 0, h->stream>>>(C3_ARGS(C3_SPEC));
+    else if (lst)
+        c3_numeric_kernel<V, false, false, true><<<grid, 256, 0, h->stream>>>(C3_ARGS(C3_NOSPEC));
     else
-        c3_numeric_kernel<V, false><<<grid, 256, 0, h->stream>>>(
-            nt, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz,
-            (const V*)A->tile_csr_Val, A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx,
-            B->tile_nnz, (const V*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,
-            (V*)C->tile_valC, C->tile_colC, nullptr, nullptr, nullptr, nullptr);
+        c3_numeric_kernel<V, false, false, false><<<grid, 256, 0, h->stream>>>(C3_ARGS(C3_NOSPEC));
+#undef C3_ARGS
+#undef C3_SPEC
+#undef C3_NOSPEC
     SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
-                       int64_t t0, int64_t t1) {
+                       int64_t t0, int64_t t1, const int* tlist) {
     if (t1 < 0) t1 = C->numtileC;
-    if (A->dtype == SPG_F64) return plain_step3_t<double>(h, A, B, C, pp, t0, t1);
-    return plain_step3_t<float>(h, A, B, C, pp, t0, t1);
+    if (A->dtype == SPG_F64) return plain_step3_t<double>(h, A, B, C, pp, t0, t1, tlist);
+    return plain_step3_t<float>(h, A, B, C, pp, t0, t1, tlist);
 }
 
 // Mixed-precision numeric (FP32 data): dense tile pairs on tensor cores, the
@@ -943,7 +971,7 @@ spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles
     unsigned* n_dense = reinterpret_cast<unsigned*>(ctr) + 3;  // high word of ctr[1]
     SPG_TRY(spg_alloc_t(h, &dense_tiles, (size_t)nt + 1));
 #define REG_ARGS                                                                                                    \
-    nt, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const float*)A->tile_csr_Val,          \
+    nt, nullptr, cv.rowidx, cv.colidx, A->tile_ptr, A->tile_columnidx, A->tile_nnz, (const float*)A->tile_csr_Val,          \
         A->tile_csr_Col, A->tile_csr_Ptr, B->csc_tile_ptr, B->csc_tile_rowidx, B->tile_nnz,                        \
         (const float*)B->tile_csr_Val, B->tile_csr_Ptr, B->mask, cv.nnz, cv.mask, cv.ptr16,                        \
         (float*)C->tile_valC, C->tile_colC

@@ -17,13 +17,22 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
                        int64_t* row_pairs, unsigned long long* pairs_total);
 spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                              int64_t* row_pairs, unsigned long long* pairs_total, const int* slot_sz);
-// Per tile-row slot sizes (predicted C tiles with margin) from the sizing MLP.
-spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz);
+// Per tile-row slot sizes (predicted C tiles with margin) from the sizing MLP
+// (slot_sz, when a model is attached) and kernel variants (rowbin: 1 plain,
+// 0 row-wise; from the exact features, refined by the model's predictions
+// when one is attached).  Either output may be null.
+spg_status mlp_predict_rows(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, int* slot_sz,
+                            uint8_t* rowbin = nullptr);
+// Step 2 over every C tile, or over the nlist tiles of tlist (ascending C
+// tile indices); tile nonzero counts into cnt32[t] (int) or, with cnt32
+// null, into cnt64[t].
 spg_status plain_step2(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                       PlainPriv* pp, int* tile_cnt);
-// Step 3 on C tiles [t0, t1) (t1 < 0: every tile).
+                       PlainPriv* pp, int* cnt32, int64_t* cnt64 = nullptr, const int* tlist = nullptr,
+                       int64_t nlist = 0);
+// Step 3 on C tiles [t0, t1) (t1 < 0: every tile), or with tlist on the
+// listed tiles tlist[t0] .. tlist[t1 - 1].
 spg_status plain_step3(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                       PlainPriv* pp, int64_t t0 = 0, int64_t t1 = -1);
+                       PlainPriv* pp, int64_t t0 = 0, int64_t t1 = -1, const int* tlist = nullptr);
 spg_status plain_step3_mixed(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, PlainPriv* pp,
                              int dense_thr, float cancel_eps, int64_t t0 = 0, int64_t t1 = -1);
 

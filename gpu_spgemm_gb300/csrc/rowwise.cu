@@ -48,12 +48,44 @@ constexpr int nw_arena() { return sizeof(ACC) == 4 ? NW_ARENA_F32 : NW_ARENA_F64
 constexpr int MAXA_SMEM = 256;  // A nonzeros per tile-row whose cursors fit in shared memory
 constexpr int SWU = 4;          // 32-product steps per sweep round of a warp (loads in flight)
 
-__device__ __forceinline__ int lower_bound_i(const int* __restrict__ a, int lo, int hi, int key) {
+// B's column at row-view position p, read from B's column array (the
+// symbolic phase) or from the interleaved {column, value} entries the numeric
+// phase reads, where one load brings a product's column and its value and
+// the segment searches pull the values into L1 for the sweep that follows.
+struct ColArray {
+    const int* ci;
+    __device__ __forceinline__ int operator()(int p) const { return __ldg(&ci[p]); }
+};
+template <typename V>
+struct BEntry;
+template <>
+struct __align__(8) BEntry<float> { int c; float v; };
+template <>
+struct __align__(16) BEntry<double> { int c; int pad; double v; };
+template <typename V>
+struct ColEntries {
+    const BEntry<V>* e;
+    __device__ __forceinline__ int operator()(int p) const { return __ldg(&e[p].c); }
+};
+
+template <typename Cols>
+__device__ __forceinline__ int lower_bound_i(Cols col, int lo, int hi, int key) {
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (__ldg(&a[mid]) < key) lo = mid + 1; else hi = mid;
+        if (col(mid) < key) lo = mid + 1; else hi = mid;
     }
     return lo;
+}
+
+template <typename V>
+__global__ void bentry_fill_kernel(int64_t nnz, const int* __restrict__ ci, const V* __restrict__ val,
+                                   BEntry<V>* __restrict__ out) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x) {
+        BEntry<V> e{};
+        e.c = ci[p];
+        e.v = val[p];
+        out[p] = e;
+    }
 }
 
 // Plan, pass 1: per C tile-row its products (sum over A's nonzeros of the B
@@ -193,17 +225,17 @@ __device__ __forceinline__ Cursors cursors_at(int* base, int stride) {
 // Cursor of every A nonzero of the tile-row: first B-row position whose column
 // is >= the region's first column, that column, and the row's end (so later
 // windows need no a_ci / b_rp loads).
+template <typename Cols>
 __device__ void init_cursors(const ItemInfo& it, Cursors cu, const int* __restrict__ colidxC,
-                             const int* __restrict__ a_ci, const int* __restrict__ b_rp,
-                             const int* __restrict__ b_ci) {
+                             const int* __restrict__ a_ci, const int* __restrict__ b_rp, Cols col) {
     const int cstart = colidxC[it.rs] * TS;
     for (int x = threadIdx.x; x < it.na; x += RW_THREADS) {
         const int k = __ldg(&a_ci[it.e0 + x]);
         int b = __ldg(&b_rp[k]);
         const int be = __ldg(&b_rp[k + 1]);
-        if (it.q > 0) b = lower_bound_i(b_ci, b, be, cstart);
+        if (it.q > 0) b = lower_bound_i(col, b, be, cstart);
         cu.pos[x] = b;
-        cu.col[x] = b < be ? __ldg(&b_ci[b]) : INT_MAX;
+        cu.col[x] = b < be ? col(b) : INT_MAX;
         cu.end[x] = be;
         cu.len[x] = 0;
     }
@@ -253,34 +285,34 @@ __device__ __forceinline__ int row_of(const int* s_rows, int e) {
 // successor, so a repeat of the last length costs one round of loads; a
 // shorter segment is found by bisection below the guess, a longer one by
 // galloping above it.  Returns the end; *nc receives the column there.
-__device__ __forceinline__ int segment_end(const int* __restrict__ b_ci, int p0, int be, int g, int pa, int pb,
-                                           int limit, int* nc) {
-    if (pa >= limit) {  // b_ci[p0] < limit <= b_ci[p0 + g - 1]
+template <typename Cols>
+__device__ __forceinline__ int segment_end(Cols col, int p0, int be, int g, int pa, int pb, int limit, int* nc) {
+    if (pa >= limit) {  // col(p0) < limit <= col(p0 + g - 1)
         int lo = p0, hi = p0 + g - 1;
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
+            if (col(mid) < limit) lo = mid; else hi = mid;
         }
-        *nc = (hi == p0 + g - 1) ? pa : __ldg(&b_ci[hi]);
+        *nc = (hi == p0 + g - 1) ? pa : col(hi);
         return hi;
     }
     if (pb >= limit) {  // exactly g entries (pb is INT_MAX at the row end)
         *nc = pb;
         return p0 + g;
     }
-    int lo = p0 + g, hi = be, step = g;  // b_ci[lo] = pb < limit
+    int lo = p0 + g, hi = be, step = g;  // col(lo) = pb < limit
     while (true) {
         const int q = lo + step;
         if (q >= be) break;
-        if (__ldg(&b_ci[q]) >= limit) { hi = q; break; }
+        if (col(q) >= limit) { hi = q; break; }
         lo = q;
         step <<= 1;
     }
-    while (hi - lo > 1) {  // b_ci[lo] < limit <= b_ci[hi] (or hi == be)
+    while (hi - lo > 1) {  // col(lo) < limit <= col(hi) (or hi == be)
         const int mid = (lo + hi) >> 1;
-        if (__ldg(&b_ci[mid]) < limit) lo = mid; else hi = mid;
+        if (col(mid) < limit) lo = mid; else hi = mid;
     }
-    *nc = hi < be ? __ldg(&b_ci[hi]) : INT_MAX;
+    *nc = hi < be ? col(hi) : INT_MAX;
     return hi;
 }
 
@@ -294,9 +326,9 @@ __device__ __forceinline__ int segment_end(const int* __restrict__ b_ci, int p0,
 // per round with all their loads in flight: consecutive lanes read
 // consecutive B entries of one segment, and a slow search stalls only its
 // own warp.  The caller synchronises the block afterwards.
-template <typename Op>
-__device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, const int* s_rows, int limit,
-                                            const int* __restrict__ b_ci, int* s_fx, Op op) {
+template <typename Op, typename Cols>
+__device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, const int* s_rows, int limit, Cols col,
+                                            int* s_fx, Op op) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     while (true) {
@@ -319,12 +351,12 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
             p0 = cu.pos[x];
             const int be = cu.end[x];
             const int g = max(1, min(cu.len[x], be - p0));
-            const int pa = g > 1 ? __ldg(&b_ci[p0 + g - 1]) : INT_MIN;
-            const int pb = p0 + g < be ? __ldg(&b_ci[p0 + g]) : INT_MAX;
+            const int pa = g > 1 ? col(p0 + g - 1) : INT_MIN;
+            const int pb = p0 + g < be ? col(p0 + g) : INT_MAX;
             ent = op.entry(x);
             r = row_of(s_rows, it.e0 + x);
             int nc;
-            const int hi = segment_end(b_ci, p0, be, g, pa, pb, limit, &nc);
+            const int hi = segment_end(col, p0, be, g, pa, pb, limit, &nc);
             len = hi - p0;
             cu.pos[x] = hi;
             cu.col[x] = nc;
@@ -360,10 +392,7 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
             typename Op::Loaded ld[SWU];
             int cc[SWU];
 #pragma unroll
-            for (int u = 0; u < SWU; u++) {
-                cc[u] = pp[u] >= 0 ? __ldg(&b_ci[pp[u]]) : 0;
-                ld[u] = op.load(pp[u]);
-            }
+            for (int u = 0; u < SWU; u++) op.fetch(pp[u], &cc[u], &ld[u]);
 #pragma unroll
             for (int u = 0; u < SWU; u++)
                 if (pp[u] >= 0) op.apply(rr[u], cc[u], ee[u], ld[u]);
@@ -372,7 +401,8 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
 }
 
 // The walk's operations: entry(x) once per active nonzero (passed between
-// lanes by shfl), load(p) per product with the round's other loads, and
+// lanes by shfl), fetch(p) per product with the round's other loads (the B
+// entry's column, and its value for the numeric product; p < 0: none), and
 // apply(r, c, entry, loaded).
 
 // Symbolic product: OR the column's bit into C's row mask.
@@ -382,9 +412,10 @@ struct SymOp {
     const uint2* bp;
     int wlo;
     uint32_t* masks32;
+    const int* b_ci;
     __device__ __forceinline__ Entry entry(int) const { return Entry{}; }
     __device__ __forceinline__ Entry shfl(Entry, int) const { return Entry{}; }
-    __device__ __forceinline__ Loaded load(int) const { return Loaded{}; }
+    __device__ __forceinline__ void fetch(int p, int* c, Loaded*) const { *c = p >= 0 ? __ldg(&b_ci[p]) : 0; }
     __device__ __forceinline__ void apply(int r, int c, Entry, Loaded) const {
         const int idx = r * WS + wrank(bp, wlo, c >> 4);
         atomicOr(&masks32[idx >> 1], (0x8000u >> (c & 15)) << ((idx & 1) * 16));
@@ -405,14 +436,21 @@ struct NumOp {
     const uint32_t* rows;
     ACC* acc;
     const V* a_val;
-    const V* b_val;
+    const BEntry<V>* bcv;
     int e0;
     __device__ __forceinline__ Entry entry(int x) const { return Entry{(ACC)__ldg(&a_val[e0 + x])}; }
     __device__ __forceinline__ Entry shfl(Entry e, int src) const {
         return Entry{__shfl_sync(0xffffffffu, e.va, src)};
     }
-    __device__ __forceinline__ Loaded load(int p) const {
-        return Loaded{p >= 0 ? (ACC)__ldg(&b_val[p]) : ACC(0)};
+    __device__ __forceinline__ void fetch(int p, int* c, Loaded* l) const {
+        if (p >= 0) {
+            const BEntry<V> e = bcv[p];
+            *c = e.c;
+            l->vb = (ACC)e.v;
+        } else {
+            *c = 0;
+            l->vb = ACC(0);
+        }
     }
     __device__ __forceinline__ void apply(int r, int c, Entry e, Loaded l) const {
         const uint32_t ti = tinfo[wrank(bp, wlo, c >> 4)].y;
@@ -430,7 +468,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
                    const int* __restrict__ a_rp, const int* __restrict__ a_ci, const int* __restrict__ b_rp,
                    const int* __restrict__ b_ci, uint16_t* __restrict__ maskC, uint8_t* __restrict__ ptrRowC,
                    int64_t* __restrict__ tile_cnt, unsigned long long* ticket, int* __restrict__ cursor_g,
-                   int max_na) {
+                   int max_na, const uint8_t* __restrict__ skip_rows) {
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* masks32 = smem;                      // [16][WS] halfwords
     int* cur_s = reinterpret_cast<int*>(masks32 + WS * 8);  // 4 x MAXA_SMEM
@@ -443,9 +481,10 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
 
     while (next_item(ticket, item_prefix, tilem, 0, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
         const ItemInfo it = s_it;
+        if (skip_rows && skip_rows[it.i]) continue;  // a tile-row the plain kernels take
         const Cursors cu = it.na <= MAXA_SMEM ? cursors_at(cur_s, MAXA_SMEM)
                                               : cursors_at(cursor_g + (int64_t)blockIdx.x * 4 * max_na, max_na);
-        init_cursors(it, cu, colidxC, a_ci, b_rp, b_ci);
+        init_cursors(it, cu, colidxC, a_ci, b_rp, ColArray{b_ci});
         for (int w0 = it.rs; w0 < it.re; w0 += WS) {
             const int nt = min(WS, it.re - w0);
             const int jlo = colidxC[w0], jhi = colidxC[w0 + nt - 1];
@@ -459,7 +498,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             }
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bp, s_sh);
-            walk_window(it, cu, s_rows, limit, b_ci, &s_fx, SymOp{bp, wlo, masks32});
+            walk_window(it, cu, s_rows, limit, ColArray{b_ci}, &s_fx, SymOp{bp, wlo, masks32, b_ci});
             __syncthreads();
             // write-out: lane pair (2j, 2j+1) takes one tile, each lane 8 of its
             // rows, so a warp's stores cover 16 tiles' contiguous masks (512 B)
@@ -512,11 +551,11 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
                   const int* __restrict__ tile_ptrC, const int* __restrict__ colidxC,
                   const int64_t* __restrict__ tile_nnzC, const uint16_t* __restrict__ maskC,
                   const uint8_t* __restrict__ ptrRowC, const int* __restrict__ a_rp, const int* __restrict__ a_ci,
-                  const V* __restrict__ a_val, const int* __restrict__ b_rp, const int* __restrict__ b_ci,
-                  const V* __restrict__ b_val, V* __restrict__ valC, uint8_t* __restrict__ colC,
+                  const V* __restrict__ a_val, const int* __restrict__ b_rp, const BEntry<V>* __restrict__ bcv,
+                  V* __restrict__ valC, uint8_t* __restrict__ colC,
                   unsigned long long* ticket, int* __restrict__ cursor_g, int max_na, int nbands,
                   const int64_t* __restrict__ band_end, unsigned* __restrict__ band_cnt,
-                  volatile int* band_flag, int band_rev, int arena) {
+                  volatile int* band_flag, int band_rev, int arena, const uint8_t* __restrict__ skip_rows) {
     extern __shared__ __align__(16) uint32_t smem[];
     const int ARENA = arena;  // bytes, a multiple of 16
     uint2* tinfo = reinterpret_cast<uint2*>(smem);  // [ntw], then rows, acc and the rank bitmap
@@ -532,8 +571,11 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
         const ItemInfo it = s_it;
         const Cursors cu = it.na <= MAXA_SMEM ? cursors_at(cur_s, MAXA_SMEM)
                                               : cursors_at(cursor_g + (int64_t)blockIdx.x * 4 * max_na, max_na);
-        init_cursors(it, cu, colidxC, a_ci, b_rp, b_ci);
-        int t0 = it.rs;
+        // a tile-row the plain kernels take: no work, but the item still
+        // counts down its band below
+        const bool skip = skip_rows && skip_rows[it.i];
+        if (!skip) init_cursors(it, cu, colidxC, a_ci, b_rp, ColEntries<V>{bcv});
+        int t0 = skip ? it.re : it.rs;
         while (t0 < it.re) {
             // window [t0, t1): the longest run of n tiles whose metadata (8 B
             // a tile, 5 B a non-empty row: at most min(values, 16 a tile)),
@@ -612,8 +654,8 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bp, s_sh);
-            walk_window(it, cu, s_rows, limit, b_ci, &s_fx,
-                        NumOp<V, ACC>{bp, wlo, tinfo, rows, acc, a_val, b_val, it.e0});
+            walk_window(it, cu, s_rows, limit, ColEntries<V>{bcv}, &s_fx,
+                        NumOp<V, ACC>{bp, wlo, tinfo, rows, acc, a_val, bcv, it.e0});
             __syncthreads();
             // column bytes: one thread per non-empty tile row writes its run;
             // values leave coalesced
@@ -677,18 +719,17 @@ size_t num_smem() {
 
 }  // namespace
 
-// AUTO: row-wise for sparse tiles (few nonzeros per tile: the per-C-tile
-// intersections and 16-wide register walks are mostly empty work), plain
-// per-C-tile register kernels for dense-ish tiles (stencils: their register
-// accumulation beats shared-memory atomics).  Measured on GB300: R-MAT 2^18
-// (1.4 nnz/tile) row-wise 77 ms vs plain 982 ms; 27-point x 3 dof (50
-// nnz/tile) plain 19 ms vs row-wise 45 ms; 2-D Poisson (16 nnz/tile) plain
-// 0.40 ms vs row-wise 0.47 ms.
-spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B) {
+// Whether the row-wise kernels can run with B's width: the symbolic kernel
+// keeps a rank bitmap as wide as B in shared memory.  AUTO then bins each
+// tile-row (mlp.cu, bin_rows_kernel): row-wise windows for sparse tiles (few
+// products per tile pair: the per-C-tile intersections and 16-wide register
+// walks are mostly empty work), the plain per-C-tile register kernels for
+// dense-ish tiles (stencils: their register accumulation beats shared-memory
+// atomics).  Measured on GB300: R-MAT 2^18 (1.4 nnz/tile) row-wise 77 ms vs
+// plain 982 ms; 27-point x 3 dof (50 nnz/tile) plain 19 ms vs row-wise 45 ms.
+bool rowwise_fits(spg_handle_t h, const spg_tiles* B) {
     const int nwords_b = (B->tilen + 31) / 32;
-    if (sym_smem(nwords_b) > h->smem_optin || num_smem<double>() > h->smem_optin) return SPG_ALGO_PLAIN;
-    const double fill = A->numtile > 0 ? (double)A->nnz / (double)A->numtile : 0.0;
-    return fill < 6.0 ? SPG_ALGO_ROWWISE : SPG_ALGO_PLAIN;
+    return sym_smem(nwords_b) <= h->smem_optin && num_smem<double>() <= h->smem_optin;
 }
 
 static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
@@ -730,7 +771,7 @@ static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles
 }
 
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
-                            int64_t* tile_cnt) {
+                            int64_t* tile_cnt, const uint8_t* skip_rows) {
     if (C->numtileC == 0) return SPG_OK;
     SPG_TRY(rw_prepare(h, A, B, C, rp));
     h->stats.work_items = rp->nitems;
@@ -744,13 +785,15 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
     rw_symbolic_kernel<<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, nwords_b, rp->item_prefix, C->tilem, rp->nitems, C->tile_ptrC, C->tile_colidxC, A->row_ptr,
-        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na);
+        A->col_idx, B->row_ptr, B->col_idx, C->maskC, C->ptrRowC, tile_cnt, rp->counters, rp->cursor_g, rp->max_na,
+        skip_rows);
     SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
 // Band reporting of one numeric launch (nbands == 0: none).
 struct BandArgs {
+    const uint8_t* skip_rows = nullptr;  // tile-rows left to the plain kernels
     int nbands = 0;
     const int64_t* band_end = nullptr;
     unsigned* band_cnt = nullptr;
@@ -794,20 +837,37 @@ static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_t
     SPG_CUDA(h, cudaFuncSetAttribute(rw_numeric_kernel<V, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters + 1, 0, sizeof(unsigned long long), h->stream));
+    // B's {column, value} entries, refreshed on every launch (a numeric
+    // re-run may come with new values on the same structure)
+    ScratchList sc(h);
+    BEntry<V>* bcv = nullptr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    SPG_CUDA(h, cudaStreamIsCapturing(h->stream, &cap));
+    if (cap == cudaStreamCaptureStatusNone)
+        SPG_TRY(spg_workspace(h, SPG_WS_BENTRY, sizeof(BEntry<V>) * ((size_t)B->nnz + 1),
+                              reinterpret_cast<void**>(&bcv)));
+    else  // inside a graph: a block of the graph's own
+        SPG_TRY(sc.alloc(&bcv, (size_t)B->nnz + 1));
+    if (B->nnz > 0) {
+        int g = (int)ceil_div(B->nnz, 256);
+        if (g > h->num_sms * 16) g = h->num_sms * 16;
+        bentry_fill_kernel<V><<<g, 256, 0, h->stream>>>(B->nnz, B->col_idx, (const V*)B->row_val, bcv);
+        SPG_LAUNCHED(h);
+    }
     int occ = 1;
     SPG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rw_numeric_kernel<V, ACC>, RW_THREADS, smem));
     const int grid = h->num_sms * (occ < 1 ? 1 : (occ > 4 ? 4 : occ));
     rw_numeric_kernel<V, ACC><<<grid, RW_THREADS, smem, h->stream>>>(
         A->m, rp->item_prefix, C->tilem, item_lo, item_hi, C->tile_ptrC, C->tile_colidxC, C->tile_nnzC,
-        C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, B->col_idx,
-        (const V*)B->row_val, (V*)C->tile_valC, C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na,
-        ba.nbands, ba.band_end, ba.band_cnt, ba.band_flag, ba.rev, arena);
+        C->maskC, C->ptrRowC, A->row_ptr, A->col_idx, (const V*)A->row_val, B->row_ptr, bcv, (V*)C->tile_valC,
+        C->tile_colC, rp->counters + 1, rp->cursor_g, rp->max_na, ba.nbands, ba.band_end, ba.band_cnt,
+        ba.band_flag, ba.rev, arena, ba.skip_rows);
     SPG_LAUNCHED(h);
     return SPG_OK;
 }
 
 spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C, RowwisePriv* rp,
-                           spg_precision prec, int r0, int r1) {
+                           spg_precision prec, int r0, int r1, const uint8_t* skip_rows) {
     if (C->numtileC == 0 || C->nnzC == 0) return SPG_OK;
     SPG_TRY(rw_prepare(h, A, B, C, rp));
     // the items of tile-rows [r0, r1); the whole range needs no device read
@@ -817,7 +877,8 @@ spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* 
     if (r0 > 0) SPG_TRY(spg_read_i64(h, rp->item_prefix + r0, &lo));
     if (r1 < C->tilem) SPG_TRY(spg_read_i64(h, rp->item_prefix + r1, &hi));
     if (hi <= lo) return SPG_OK;
-    const BandArgs none{};
+    BandArgs none{};
+    none.skip_rows = skip_rows;
     if (A->dtype == SPG_F64) return launch_numeric<double, double>(h, A, B, C, rp, lo, hi, none);
     if (prec == SPG_PREC_F64) return launch_numeric<float, double>(h, A, B, C, rp, lo, hi, none);
     return launch_numeric<float, float>(h, A, B, C, rp, lo, hi, none);
@@ -826,7 +887,7 @@ spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* 
 spg_status rowwise_numeric_bands_launch(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                                         RowwisePriv* rp, spg_precision prec, int nbands, const int* d_rows,
                                         int64_t* d_band_end, unsigned* d_band_cnt, volatile int* band_flag_dev,
-                                        int64_t* h_band_end, bool last_first) {
+                                        int64_t* h_band_end, bool last_first, const uint8_t* skip_rows) {
     SPG_TRY(rw_prepare(h, A, B, C, rp));
     band_plan_kernel<<<(nbands + 255) / 256, 256, 0, h->stream>>>(nbands, d_rows, rp->item_prefix, d_band_end,
                                                                   d_band_cnt);
@@ -836,6 +897,7 @@ spg_status rowwise_numeric_bands_launch(spg_handle_t h, const spg_tiles* A, cons
     SPG_CUDA(h, cudaStreamSynchronize(h->stream));
     if (C->numtileC == 0 || C->nnzC == 0 || rp->nitems == 0) return SPG_OK;
     BandArgs ba;
+    ba.skip_rows = skip_rows;
     ba.nbands = nbands;
     ba.band_end = d_band_end;
     ba.band_cnt = d_band_cnt;

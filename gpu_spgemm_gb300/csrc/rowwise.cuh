@@ -12,12 +12,15 @@ struct RowwisePriv {
     int grid = 0;
 };
 
-spg_algo rowwise_choose(spg_handle_t h, const spg_tiles* A, const spg_tiles* B);
+bool rowwise_fits(spg_handle_t h, const spg_tiles* B);
+// skip_rows (optional, tilem flags): tile-rows whose work items are skipped
+// (the binned algorithm leaves them to the plain kernels).
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                            RowwisePriv* rp, int64_t* tile_cnt);
+                            RowwisePriv* rp, int64_t* tile_cnt, const uint8_t* skip_rows = nullptr);
 // Numeric phase on C tile-rows [r0, r1) (r1 < 0: every tile-row).
 spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
-                           RowwisePriv* rp, spg_precision prec, int r0 = 0, int r1 = -1);
+                           RowwisePriv* rp, spg_precision prec, int r0 = 0, int r1 = -1,
+                           const uint8_t* skip_rows = nullptr);
 // One numeric launch over every tile-row that reports bands of tile-rows as
 // they complete: band k = tile-rows [rows[k], rows[k+1]) (d_rows on the
 // device, nbands + 1 entries).  Fills h_band_end[k] (first work item after
@@ -28,6 +31,6 @@ spg_status rowwise_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* 
 spg_status rowwise_numeric_bands_launch(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                                         RowwisePriv* rp, spg_precision prec, int nbands, const int* d_rows,
                                         int64_t* d_band_end, unsigned* d_band_cnt, volatile int* band_flag_dev,
-                                        int64_t* h_band_end, bool last_first);
+                                        int64_t* h_band_end, bool last_first, const uint8_t* skip_rows = nullptr);
 void rowwise_free_priv(spg_handle_t h, RowwisePriv* rp);
 void rowwise_free_bview(spg_handle_t h, spg_tiles* t);

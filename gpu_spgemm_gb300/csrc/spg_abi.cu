@@ -26,6 +26,11 @@ struct CPriv {
     spg_algo algo = SPG_ALGO_PLAIN;
     RowwisePriv rw;
     bool vals_joint = false;       // tile_colC lives inside tile_valC's allocation
+    // SPG_ALGO_BINNED: the tile-rows the plain kernels take
+    uint8_t* rowbin = nullptr;     // tilem: 1 = plain kernels, 0 = row-wise windows
+    int64_t* plain_off = nullptr;  // tilem+1: prefix of the plain tile-rows' C tiles
+    int* plain_list = nullptr;     // those C tiles, ascending
+    int64_t nplain = 0;
 };
 
 RowwisePriv* ctiles_rowwise_priv(spg_ctiles* C) {
@@ -63,6 +68,21 @@ void spg_free_async(spg_handle_t h, void* p) {
     if (p) cudaFreeAsync(p, h->stream);
 }
 
+spg_status spg_workspace(spg_handle_t h, int kind, size_t bytes, void** out) {
+    if (kind < 0 || kind >= (int)(sizeof(h->ws) / sizeof(h->ws[0])))
+        return spg_fail(h, SPG_ERR_INVALID, "internal: bad workspace kind");
+    if (bytes > h->ws_bytes[kind]) {
+        spg_free_async(h, h->ws[kind]);
+        h->ws[kind] = nullptr;
+        h->ws_bytes[kind] = 0;
+        const size_t grow = bytes + bytes / 8;  // some headroom for the next, slightly larger, call
+        SPG_TRY(spg_alloc(h, &h->ws[kind], grow));
+        h->ws_bytes[kind] = grow;
+    }
+    *out = h->ws[kind];
+    return SPG_OK;
+}
+
 spg_status spg_read_i64(spg_handle_t h, const int64_t* d, int64_t* out) {
     SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned, d, sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
     SPG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -77,9 +97,8 @@ spg_status spg_read_i32(spg_handle_t h, const int* d, int* out) {
     return SPG_OK;
 }
 
-spg_status spg_check_flags(spg_handle_t h, const char* where) {
-    SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 1, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
-    SPG_CUDA(h, cudaStreamSynchronize(h->stream));
+// Turns device error bits read back into h_pinned[1] into a status.
+static spg_status flags_status(spg_handle_t h, const char* where) {
     const unsigned f = *reinterpret_cast<unsigned*>(h->h_pinned + 1);
     if (f == 0) return SPG_OK;
     SPG_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
@@ -90,6 +109,25 @@ spg_status spg_check_flags(spg_handle_t h, const char* where) {
     if (f & DERR_TOO_BIG) return spg_fail(h, SPG_ERR_INVALID, w + ": a count overflowed its index type");
     if (f & DERR_OVERFLOW) return spg_fail(h, SPG_ERR_OVERFLOW_RERUN, w + ": a pre-sized buffer overflowed");
     return spg_fail(h, SPG_ERR_CUDA, w + ": unknown device error");
+}
+
+spg_status spg_check_flags(spg_handle_t h, const char* where) {
+    SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 1, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    SPG_CUDA(h, cudaStreamSynchronize(h->stream));
+    return flags_status(h, where);
+}
+
+// n (<= 8) device int64 scalars and the device error bits in one round trip:
+// the stream's work so far is complete when this returns.
+spg_status spg_read_i64s_checked(spg_handle_t h, int n, const int64_t* const* src, int64_t* out, const char* where) {
+    SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 1, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    for (int k = 0; k < n; k++)
+        SPG_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8 + k, src[k], sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    h->stream));
+    SPG_CUDA(h, cudaStreamSynchronize(h->stream));
+    SPG_TRY(flags_status(h, where));
+    for (int k = 0; k < n; k++) out[k] = h->h_pinned[8 + k];
+    return SPG_OK;
 }
 
 extern "C" spg_status spg_create(spg_handle_t* out, int device, void* stream) {
@@ -126,6 +164,7 @@ extern "C" spg_status spg_create(spg_handle_t* out, int device, void* stream) {
 
 extern "C" spg_status spg_destroy(spg_handle_t h) {
     if (!h) return SPG_ERR_INVALID;
+    for (void* p : h->ws) spg_free_async(h, p);
     cudaStreamSynchronize(h->stream);
     for (auto& ev : h->ev) cudaEventDestroy(ev);
     cudaFree(h->d_flags);
@@ -231,6 +270,16 @@ static spg_status validate_pair(spg_handle_t h, const spg_tiles* A, const spg_ti
     return SPG_OK;
 }
 
+// Whether a pair cache of `bytes` leaves enough device memory: small caches
+// always do (no query); larger ones may take a quarter of the free memory.
+static bool cache_fits(spg_handle_t h, size_t bytes) {
+    (void)h;
+    if (bytes <= ((size_t)1 << 30)) return true;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return false;
+    return bytes < fr / 4;
+}
+
 static float elapsed(spg_handle_t h, int a, int b) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]);
@@ -246,7 +295,7 @@ extern "C" spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C) {
     if (C->priv) {
         CPriv* cp = static_cast<CPriv*>(C->priv);
         void* pp[] = {cp->plain.spec_cnt, cp->plain.spec_off, cp->plain.spec_pa, cp->plain.spec_pb,
-                      cp->plain.counters, cp->row_pairs};
+                      cp->plain.counters, cp->row_pairs, cp->rowbin, cp->plain_off, cp->plain_list};
         for (void* p : pp) spg_free_async(h, p);
         rowwise_free_priv(h, &cp->rw);
         delete cp;
@@ -255,20 +304,93 @@ extern "C" spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C) {
     return SPG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// SPG_ALGO_BINNED: the C tiles of the tile-rows binned to the plain kernels
+// ---------------------------------------------------------------------------
+__global__ void plain_count_kernel(int tilem, const uint8_t* __restrict__ rowbin, const int* __restrict__ tile_ptrC,
+                                   int* __restrict__ cnt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x)
+        cnt[i] = rowbin[i] ? tile_ptrC[i + 1] - tile_ptrC[i] : 0;
+}
+
+__global__ void plain_list_kernel(int tilem, const uint8_t* __restrict__ rowbin, const int* __restrict__ tile_ptrC,
+                                  const int64_t* __restrict__ off, int* __restrict__ list) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < tilem; i += nw) {
+        if (!rowbin[i]) continue;
+        const int t0 = tile_ptrC[i], n = tile_ptrC[i + 1] - t0;
+        for (int k = lane; k < n; k += 32) list[off[i] + k] = t0 + k;
+    }
+}
+
+static int small_grid(spg_handle_t h, int64_t units, int per_block) {
+    int64_t g = ceil_div(units, per_block);
+    if (g > (int64_t)h->num_sms * 8) g = (int64_t)h->num_sms * 8;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// After step 1 of a binned product: the plain tile-rows' C tiles as a list.
+// A product whose tile-rows all went one way runs that algorithm alone.
+static spg_status bin_tiles(spg_handle_t h, spg_ctiles* C, CPriv* cp, spg_algo* algo) {
+    const int tilem = C->tilem;
+    ScratchList sc(h);
+    int* cnt = nullptr;
+    SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
+    SPG_TRY(spg_alloc_t(h, &cp->plain_off, (size_t)tilem + 1));
+    if (tilem > 0) {
+        plain_count_kernel<<<small_grid(h, tilem, 256), 256, 0, h->stream>>>(tilem, cp->rowbin, C->tile_ptrC, cnt);
+        SPG_LAUNCHED(h);
+    }
+    SPG_TRY(spg_scan_i32_to_i64(h, cnt, cp->plain_off, tilem));
+    SPG_TRY(spg_read_i64(h, cp->plain_off + tilem, &cp->nplain));
+    if (cp->nplain == 0 || cp->nplain == C->numtileC) {
+        *algo = cp->nplain == 0 ? SPG_ALGO_ROWWISE : SPG_ALGO_PLAIN;
+        spg_free_async(h, cp->rowbin);
+        spg_free_async(h, cp->plain_off);
+        cp->rowbin = nullptr;
+        cp->plain_off = nullptr;
+        cp->nplain = 0;
+        return SPG_OK;
+    }
+    SPG_TRY(spg_alloc_t(h, &cp->plain_list, (size_t)cp->nplain + 1));
+    plain_list_kernel<<<small_grid(h, (int64_t)tilem * 32, 256), 256, 0, h->stream>>>(tilem, cp->rowbin,
+                                                                                        C->tile_ptrC, cp->plain_off,
+                                                                                        cp->plain_list);
+    SPG_LAUNCHED(h);
+    return SPG_OK;
+}
+
 // Step 1: C's tile structure (tile_ptrC, tile_rowidxC, tile_colidxC).
+// final: step 1 alone (spg_symbolic_tiles) -- wait for it and check its
+// device errors here; otherwise step 2's read-back does both.
 static spg_status tiles_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
-                             spg_ctiles* C) {
+                             spg_ctiles* C, bool final) {
     *C = spg_ctiles{};
     C->m = A->m; C->n = B->n; C->tilem = A->tilem; C->tilen = B->tilen; C->dtype = A->dtype;
     CPriv* cp = new (std::nothrow) CPriv();
     if (!cp) return spg_fail(h, SPG_ERR_OOM, "host allocation failed");
     C->priv = cp;
-    if (algo == SPG_ALGO_AUTO) algo = rowwise_choose(h, A, B);
-    cp->algo = algo;
-    h->stats.algo_used = (int32_t)algo;
+    // AUTO: each tile-row to the plain or the row-wise kernels (below).  On a
+    // small A (under 65,536 tiles) one choice for the whole product, by A's
+    // nonzeros per tile: binning costs a features pass and a read-back that
+    // such a product cannot win back.  The row-wise kernels need B narrow
+    // enough for their shared memory.
+    if (algo == SPG_ALGO_AUTO) {
+        if (!rowwise_fits(h, B))
+            algo = SPG_ALGO_PLAIN;
+        else if (A->numtile >= 65536)
+            algo = SPG_ALGO_BINNED;
+        else
+            algo = A->numtile > 0 && (double)A->nnz / (double)A->numtile < 6.0 ? SPG_ALGO_ROWWISE : SPG_ALGO_PLAIN;
+    } else if (algo == SPG_ALGO_BINNED && !rowwise_fits(h, B)) {
+        algo = SPG_ALGO_PLAIN;
+    }
+    const bool binned = algo == SPG_ALGO_BINNED;
     SPG_TRY(spg_alloc_t(h, &cp->plain.counters, 4));
     SPG_CUDA(h, cudaMemsetAsync(cp->plain.counters, 0, 4 * sizeof(unsigned long long), h->stream));
     SPG_TRY(spg_alloc_t(h, &cp->row_pairs, (size_t)A->tilem + 1));
+    if (binned) SPG_TRY(spg_alloc_t(h, &cp->rowbin, (size_t)A->tilem + 16));
     SPG_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
     // ---- step 1: C tile structure
     if (h->sizing) {
@@ -277,7 +399,7 @@ static spg_status tiles_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
             ScratchList sc(h);
             int* slot = nullptr;
             st = sc.alloc(&slot, (size_t)A->tilem + 1);
-            if (st == SPG_OK) st = mlp_predict_rows(h, A, B, slot);
+            if (st == SPG_OK) st = mlp_predict_rows(h, A, B, slot, cp->rowbin);
             if (st == SPG_OK) st = plain_step1_sized(h, A, B, C, cp->row_pairs, cp->plain.counters + 2, slot);
         }
         if (st == SPG_ERR_OOM) {
@@ -297,12 +419,17 @@ static spg_status tiles_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
             SPG_TRY(st);
         }
     } else {
+        if (binned) SPG_TRY(mlp_predict_rows(h, A, B, nullptr, cp->rowbin));
         SPG_TRY(plain_step1(h, A, B, C, cp->row_pairs, cp->plain.counters + 2));
     }
+    if (binned) SPG_TRY(bin_tiles(h, C, cp, &algo));
+    cp->algo = algo;
+    h->stats.algo_used = (int32_t)algo;
     SPG_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
-    SPG_CUDA(h, cudaEventSynchronize(h->ev[1]));
+    if (!final) return SPG_OK;  // step 2 follows: its read-back checks both steps
+    SPG_TRY(spg_check_flags(h, "symbolic step 1"));
     h->stats.ms_step1 = elapsed(h, 0, 1);
-    return spg_check_flags(h, "symbolic step 1");
+    return SPG_OK;
 }
 
 // Step 2 on C's tile structure from tiles_impl: masks, row offsets, tile
@@ -310,7 +437,7 @@ static spg_status tiles_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
 static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C) {
     CPriv* cp = static_cast<CPriv*>(C->priv);
     const spg_algo algo = cp->algo;
-    SPG_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+    SPG_CUDA(h, cudaEventRecord(h->ev[7], h->stream));
     const int64_t nt = C->numtileC;
     // ---- step 2: bitmask symbolic
     int* tile_cnt = nullptr;
@@ -321,16 +448,31 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         // tile counts land in tile_nnzC itself and are scanned in place
         SPG_TRY(rowwise_symbolic(h, A, B, C, &cp->rw, C->tile_nnzC));
         SPG_TRY(spg_scan_i64_to_i64(h, C->tile_nnzC, C->tile_nnzC, nt));
+    } else if (algo == SPG_ALGO_BINNED) {
+        // the row-wise tile-rows, then the plain kernels over the listed
+        // tiles; both leave tile counts in tile_nnzC, scanned in place.  The
+        // pair cache covers the listed tiles; every other tile reads "not
+        // cached" (-1) and intersects its lists if a plain kernel meets it.
+        SPG_TRY(rowwise_symbolic(h, A, B, C, &cp->rw, C->tile_nnzC, cp->rowbin));
+        const int64_t cap = 8 * cp->nplain;
+        if (cache_fits(h, (size_t)cap * 8 + (size_t)nt * 8)) {
+            cp->plain.spec_cap = cap;
+            SPG_TRY(spg_alloc_t(h, &cp->plain.spec_cnt, (size_t)nt + 1));
+            SPG_TRY(spg_alloc_t(h, &cp->plain.spec_off, (size_t)nt + 1));
+            SPG_TRY(spg_alloc_t(h, &cp->plain.spec_pa, (size_t)cap + 1));
+            SPG_TRY(spg_alloc_t(h, &cp->plain.spec_pb, (size_t)cap + 1));
+            SPG_CUDA(h, cudaMemsetAsync(cp->plain.spec_cnt, 0xff, sizeof(int) * ((size_t)nt + 1), h->stream));
+        }
+        SPG_TRY(plain_step2(h, A, B, C, &cp->plain, nullptr, C->tile_nnzC, cp->plain_list, cp->nplain));
+        SPG_TRY(spg_scan_i64_to_i64(h, C->tile_nnzC, C->tile_nnzC, nt));
     } else {
         SPG_TRY(spg_alloc_t(h, &tile_cnt, (size_t)nt + 1));
-        size_t fr = 0, tot = 0;
-        cudaMemGetInfo(&fr, &tot);
         int64_t cap = 8 * nt;  // src/spgemm_raw_v2.cu:170
         if (const char* d = getenv("SPG_SPEC_CAP_DIV")) {  // test knob: force the overflow re-run
             const long div = atol(d);
             if (div > 1) cap = cap / div > 0 ? cap / div : 1;
         }
-        if (cap > 0 && (size_t)cap * 8 + (size_t)nt * 8 < fr / 4) {
+        if (cap > 0 && cache_fits(h, (size_t)cap * 8 + (size_t)nt * 8)) {
             cp->plain.spec_cap = cap;
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_cnt, (size_t)nt + 1));
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_off, (size_t)nt + 1));
@@ -341,12 +483,16 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         SPG_TRY(spg_scan_i32_to_i64(h, tile_cnt, C->tile_nnzC, nt));
         spg_free_async(h, tile_cnt);
     }
-    SPG_TRY(spg_read_i64(h, C->tile_nnzC + nt, &C->nnzC));
-    {
-        int64_t pairs = 0;
-        SPG_TRY(spg_read_i64(h, (const int64_t*)(cp->plain.counters + 2), &pairs));
-        C->pairs = pairs;
+    SPG_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+    {   // nnzC, the tile pairs and both steps' device errors in one round trip
+        const int64_t* src[2] = {C->tile_nnzC + nt, (const int64_t*)(cp->plain.counters + 2)};
+        int64_t v[2] = {0, 0};
+        SPG_TRY(spg_read_i64s_checked(h, 2, src, v, "symbolic"));
+        C->nnzC = v[0];
+        C->pairs = v[1];
     }
+    if (!h->stats.ms_step1) h->stats.ms_step1 = elapsed(h, 0, 1);
+    h->stats.ms_step2 = elapsed(h, 7, 2);
     const size_t vs = val_size(C->dtype);
     {   // values and column bytes in one allocation: a repeated product of the
         // same size then reuses one pooled block instead of splitting others
@@ -355,15 +501,12 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         C->tile_colC = static_cast<uint8_t*>(C->tile_valC) + vbytes;
         cp->vals_joint = true;
     }
-    SPG_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
-    SPG_CUDA(h, cudaEventSynchronize(h->ev[2]));
-    h->stats.ms_step2 = elapsed(h, 1, 2);
-    return spg_check_flags(h, "symbolic");
+    return SPG_OK;
 }
 
 static spg_status symbolic_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                                 spg_ctiles* C) {
-    SPG_TRY(tiles_impl(h, A, B, algo, C));
+    SPG_TRY(tiles_impl(h, A, B, algo, C, false));
     return masks_impl(h, A, B, C);
 }
 
@@ -385,11 +528,20 @@ extern "C" spg_status spg_set_mixed_params(spg_handle_t h, int dense_thr, float 
     return SPG_OK;
 }
 
+extern "C" spg_status spg_set_bin_params(spg_handle_t h, float pp_thr, float fill_thr) {
+    if (!h) return SPG_ERR_INVALID;
+    if (!(pp_thr >= 0.f) || !(fill_thr >= 0.f) || pp_thr > 1e9f || fill_thr > 256.f)
+        return spg_fail(h, SPG_ERR_INVALID, "bin params: pp_thr in [0, 1e9], fill_thr in [0, 256]");
+    h->bin_pp_thr = pp_thr;
+    h->bin_fill_thr = fill_thr;
+    return SPG_OK;
+}
+
 extern "C" spg_status spg_symbolic_tiles(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                                          spg_ctiles* C) {
     SPG_TRY(validate_pair(h, A, B, C));
     h->stats = spg_stats{};
-    spg_status s = tiles_impl(h, A, B, algo, C);
+    spg_status s = tiles_impl(h, A, B, algo, C, true);
     if (s != SPG_OK) { std::string e = h->err; spg_ctiles_free(h, C); h->err = e; }
     return s;
 }
@@ -406,7 +558,7 @@ extern "C" spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, con
 // Step 3 on C tile-rows [r0, r1).
 // The kernels step 3 runs on: row-wise windows, plain per-C-tile registers,
 // or plain with dense pairs on the tensor cores.
-enum class NumPath { ROWWISE, PLAIN, MIXED };
+enum class NumPath { ROWWISE, PLAIN, MIXED, BINNED };
 
 // Checks that C is ready for step 3 (symbolic structure and masks) and picks
 // its path: MIXED for SPG_PREC_MIXED on FP32 data; ROWWISE when C's structure
@@ -420,11 +572,19 @@ static spg_status numeric_path(spg_handle_t h, const spg_tiles* A, const spg_til
         return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
     const CPriv* cp = static_cast<const CPriv*>(C->priv);
     if (algo == SPG_ALGO_AUTO) algo = cp->algo;
-    if (algo == SPG_ALGO_ROWWISE && cp->algo != SPG_ALGO_ROWWISE) algo = SPG_ALGO_PLAIN;
+    // the row-wise kernels need their plan, made by a row-wise or binned symbolic phase
+    const bool rw_plan = cp->algo == SPG_ALGO_ROWWISE || cp->algo == SPG_ALGO_BINNED;
+    if ((algo == SPG_ALGO_ROWWISE || algo == SPG_ALGO_BINNED) && !rw_plan) algo = SPG_ALGO_PLAIN;
+    if (algo == SPG_ALGO_BINNED && cp->algo != SPG_ALGO_BINNED) algo = cp->algo;
     if (prec == SPG_PREC_MIXED && A->dtype == SPG_F32)
         *path = NumPath::MIXED;
-    else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32))
-        *path = NumPath::ROWWISE;
+    else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32 && rw_plan))
+        *path = NumPath::ROWWISE;  // FP64 accumulation of FP32 data: the row-wise kernels, every tile-row
+    else if (prec == SPG_PREC_F64 && A->dtype == SPG_F32)
+        return spg_fail(h, SPG_ERR_UNSUPPORTED,
+                        "numeric: FP64 accumulation of FP32 data needs a row-wise or binned symbolic phase");
+    else if (algo == SPG_ALGO_BINNED)
+        *path = NumPath::BINNED;
     else
         *path = NumPath::PLAIN;
     return SPG_OK;
@@ -441,6 +601,14 @@ static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_til
     const bool mixed = path == NumPath::MIXED;
     if (path == NumPath::ROWWISE) {
         SPG_TRY(rowwise_numeric(h, A, B, C, &cp->rw, prec, r0, r1));
+    } else if (path == NumPath::BINNED) {
+        int64_t l0 = 0, l1 = cp->nplain;  // the listed tiles of tile-rows [r0, r1)
+        if (!whole) {
+            SPG_TRY(spg_read_i64(h, cp->plain_off + r0, &l0));
+            SPG_TRY(spg_read_i64(h, cp->plain_off + r1, &l1));
+        }
+        SPG_TRY(plain_step3(h, A, B, C, &cp->plain, l0, l1, cp->plain_list));
+        SPG_TRY(rowwise_numeric(h, A, B, C, &cp->rw, prec, r0, r1, cp->rowbin));
     } else {
         int64_t t0 = 0, t1 = C->numtileC;  // C tiles of the tile-rows
         if (!whole) {
@@ -456,9 +624,9 @@ static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_til
             SPG_TRY(plain_step3(h, A, B, C, &cp->plain, t0, t1));
     }
     SPG_CUDA(h, cudaEventRecord(h->ev[4], h->stream));
-    SPG_CUDA(h, cudaEventSynchronize(h->ev[4]));
+    SPG_TRY(spg_check_flags(h, "numeric"));  // waits for the stream, so ev[4] is done
     h->stats.ms_step3 = elapsed(h, 3, 4);
-    return spg_check_flags(h, "numeric");
+    return SPG_OK;
 }
 
 extern "C" spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
@@ -488,7 +656,7 @@ extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, cons
     NumPath path;
     SPG_TRY(numeric_path(h, A, B, algo, prec, C, &path));
     CPriv* cp = static_cast<CPriv*>(C->priv);
-    if (path != NumPath::ROWWISE) {
+    if (path != NumPath::ROWWISE && path != NumPath::BINNED) {
         float ms = 0.f;
         for (int j = 0; j < nbands; j++) {
             const int k = last_first ? nbands - 1 - j : j;
@@ -532,8 +700,12 @@ extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, cons
                                 h->stream));
     std::vector<int64_t> end((size_t)nbands);
     SPG_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
+    // binned: the plain kernels' tiles first (one launch), so a band is
+    // complete once the row-wise items of its tile-rows are
+    if (path == NumPath::BINNED) SPG_TRY(plain_step3(h, A, B, C, &cp->plain, 0, cp->nplain, cp->plain_list));
     const spg_status ls = rowwise_numeric_bands_launch(h, A, B, C, &cp->rw, prec, nbands, d_rows, d_end, d_cnt,
-                                                       h->d_band, end.data(), last_first);
+                                                       h->d_band, end.data(), last_first,
+                                                       path == NumPath::BINNED ? cp->rowbin : nullptr);
     if (ls != SPG_OK) return ls;
     SPG_CUDA(h, cudaEventRecord(h->ev[4], h->stream));
     std::vector<char> told((size_t)nbands, 0);

@@ -89,6 +89,10 @@ struct spg_handle_s {
     size_t smem_optin = 0;
     size_t smem_per_sm = 0;
     int64_t launches = 0;             // kernels launched through this handle
+    void* ws[4] = {};                 // grow-only workspaces of the large per-call temporaries
+    size_t ws_bytes[4] = {};
+    float bin_pp_thr = 12.0f;          // binned algorithm: products per tile pair for the plain kernels
+    float bin_fill_thr = 16.0f;       // ... and predicted C nonzeros per C tile (with a sizing model)
 };
 
 spg_status spg_fail(spg_handle_t h, spg_status s, const std::string& msg);
@@ -154,8 +158,20 @@ class ScratchList {
     int n_ = 0;
 };
 
+// A large temporary that every call of a kind needs (the learned slots of
+// step 1, B's interleaved entries of the numeric phase) lives in a grow-only
+// buffer of the handle instead of a fresh pool block per call: a repeated
+// product then allocates only C's own arrays, the same blocks each time.
+// Uses are ordered on the handle's stream, so one call's use ends before the
+// next begins; spg_destroy releases the buffers.  Not for work captured into
+// a CUDA graph (a later growth would move the buffer under the graph).
+enum { SPG_WS_SLOTS = 0, SPG_WS_BENTRY = 1 };
+spg_status spg_workspace(spg_handle_t h, int kind, size_t bytes, void** out);
+
 // Read device error bits (synchronises the stream) and clear them.
 spg_status spg_check_flags(spg_handle_t h, const char* where);
+// n (<= 8) device int64 scalars and the error bits in one round trip.
+spg_status spg_read_i64s_checked(spg_handle_t h, int n, const int64_t* const* src, int64_t* out, const char* where);
 
 // Exclusive scans: out[0..n] (n+1 entries, out[n] = total).  `in` may alias
 // `out` when the types match.  Temporary storage comes from spg_alloc.

@@ -256,6 +256,29 @@ def smoothed_aggregation(a: CSR, p0: CSR, omega: float = 2.0 / 3.0) -> CSR:
     return CSR.from_scipy(P, dtype=a.val.dtype)
 
 
+def block_diag(*blocks: CSR) -> CSR:
+    """The block-diagonal matrix of the given CSR blocks (values cast to the
+    first block's type): a product of it with itself is the independent
+    products of its blocks side by side, each block keeping its own
+    character (a stencil beside a power-law graph, for instance)."""
+    dtype = blocks[0].val.dtype
+    m = sum(b.m for b in blocks)
+    n = sum(b.n for b in blocks)
+    rps, cis, vals = [np.zeros(1, np.int64)], [], []
+    r_off = c_off = nz_off = 0
+    for b in blocks:
+        rps.append(b.row_ptr[1:].astype(np.int64) + nz_off)
+        cis.append(b.col_idx.astype(np.int64) + c_off)
+        vals.append(b.val.astype(dtype))
+        r_off += b.m
+        c_off += b.n
+        nz_off += b.nnz
+    rp = np.concatenate(rps)
+    if rp[-1] >= 2**31:
+        raise ValueError("nnz exceeds int32 CSR indexing")
+    return CSR(m, n, rp.astype(np.int32), np.concatenate(cis).astype(np.int32), np.concatenate(vals))
+
+
 def transpose(a: CSR) -> CSR:
     """Host CSR transpose with stable (row-ascending) order inside each column,
     the same order the reference's ``--aat`` path builds (src/spgemm_raw_v2.cu:79-90)."""

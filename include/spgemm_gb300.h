@@ -55,11 +55,17 @@ typedef enum { SPG_LAYOUT_ROW = 0, SPG_LAYOUT_B_CSC = 1 } spg_layout;
 /* spg_tile_from_csr flags */
 #define SPG_TILE_WITH_TILE_CSC 0x1   /* also build tile_csc_Ptr/Row/Val (B only) */
 
-/* Numeric algorithms.  PLAIN: one warp per C tile, matched tile pairs by list
-   intersection, register accumulators (the reference's step 3 structure).
-   ROWWISE: tile-row work items in shared-memory windows, binned by density.
-   AUTO picks per workload. */
-typedef enum { SPG_ALGO_AUTO = 0, SPG_ALGO_PLAIN = 1, SPG_ALGO_ROWWISE = 2 } spg_algo;
+/* Algorithms of steps 2 and 3.  PLAIN: one warp per C tile, matched tile
+   pairs by list intersection, register accumulators (the reference's
+   structure).  ROWWISE: tile-row work items in shared-memory windows.
+   BINNED: each C tile-row to one of the two, by its products per tile pair
+   and, with a sizing model attached (spg_set_sizing_model), by the model's
+   predicted C nonzeros per C tile (spg_set_bin_params); a product whose
+   tile-rows all bin one way runs that algorithm alone.  AUTO is BINNED
+   for an A of at least 65,536 tiles; for a smaller A it picks one of the two
+   for the whole product by A's nonzeros per tile (ROWWISE below 6); PLAIN
+   where B is too wide for the row-wise kernels' shared memory. */
+typedef enum { SPG_ALGO_AUTO = 0, SPG_ALGO_PLAIN = 1, SPG_ALGO_ROWWISE = 2, SPG_ALGO_BINNED = 3 } spg_algo;
 
 /* Precision of the numeric phase for FP32 inputs.  F32: FP32 register path.
    MIXED: FP32 bulk, tiles above the fill threshold on BF16/FP16 tensor cores
@@ -180,6 +186,13 @@ spg_status spg_tiles_free(spg_handle_t h, spg_tiles* t);
  * A must be SPG_LAYOUT_ROW, B SPG_LAYOUT_B_CSC, A.n == B.m, same dtype. */
 spg_status spg_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                         spg_ctiles* C);
+
+/* SPG_ALGO_BINNED thresholds: a tile-row runs the plain kernels when its
+ * products per matched tile pair reach pp_thr (default 12) and, with a sizing
+ * model attached, its predicted C nonzeros per predicted C tile reach
+ * fill_thr (default 16).  No reference counterpart (the reference runs one
+ * kernel configuration for every tile-row, src/spgemm_raw_kernels.cuh:9-14). */
+spg_status spg_set_bin_params(spg_handle_t h, float pp_thr, float fill_thr);
 
 /* SPG_PREC_MIXED parameters: tile pairs whose A and B tiles both hold >=
  * dense_thr nonzeros run on the tensor cores (default 32); C tiles with an

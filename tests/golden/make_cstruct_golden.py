@@ -14,6 +14,8 @@ launch stays inside its buffers.
 
 Run on a GPU host from the repository root (writes to the given directory):
     python tests/golden/make_cstruct_golden.py OUT_DIR
+With --time instead it times those kernels on the benchmark configurations
+they can run (see time_reference).
 """
 from __future__ import annotations
 
@@ -60,6 +62,8 @@ class Driver:
         if r != 0:
             raise RuntimeError(f"{what} failed with CUresult {r}")
 
+    timings = None  # name -> list of ms, when timing
+
     def launch(self, name, grid, block, smem, args):
         holders = []
         for a in args:
@@ -68,8 +72,17 @@ class Driver:
             else:  # torch tensor or None
                 holders.append(C.c_void_p(a.data_ptr() if a is not None else 0))
         arr = (C.c_void_p * len(holders))(*[C.cast(C.pointer(h), C.c_void_p) for h in holders])
+        ev = None
+        if self.timings is not None:
+            ev = [self.torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            self.torch.cuda.synchronize()
+            ev[0].record()
         self._ck(self.cu.cuLaunchKernel(self.fn[name], grid, 1, 1, block, 1, 1, smem, None, arr, None), name)
+        if ev is not None:
+            ev[1].record()
         self._ck(self.cu.cuCtxSynchronize(), name + " sync")
+        if ev is not None:
+            self.timings.setdefault(name, []).append(ev[0].elapsed_time(ev[1]))
 
     def dev(self, x):
         x = np.ascontiguousarray(x)
@@ -157,7 +170,37 @@ def run_case(d: Driver, a, b):
     return out
 
 
+def time_reference(reps: int = 5):
+    """Kernel times of the reference's own steps 1-3 on the two benchmark
+    configurations they can run (FP64, their only value type): the 2-D
+    5-point Poisson 256^2 and the 27-point stencil 64^3 x 3 dof.  Each kernel
+    is bracketed by CUDA events on the default stream (host scans, copies and
+    allocations between them are not counted, so the sum is a lower bound on
+    the reference's step time).  Prints one JSON line per configuration."""
+    import json
+    from gpu_spgemm_gb300 import synth
+    d = Driver()
+    for name, a in (("poisson2d_256_f64", synth.poisson2d(256)),
+                    ("stencil27_64_dof3_f64", synth.stencil27_dof3(64, dtype=np.float64))):
+        d.timings = None
+        run_case(d, a, a)  # warm-up, and the oracle's pair count sizes the cache
+        d.timings = {}
+        for _ in range(reps):
+            run_case(d, a, a)
+        per = {k: float(np.median(v)) for k, v in d.timings.items()}
+        steps = {"step1": per.get("step1_count", 0) + per.get("step1_fill", 0),
+                 "step2": per.get("step2_symbolic", 0) + per.get("step2_ptrRowC", 0),
+                 "step3": per.get("step3_numeric_v2", 0)}
+        ms = sum(steps.values())
+        prods = synth.products(a, a)
+        print(json.dumps({"reference_kernels": name, "products": prods, "kernel_ms": per, "step_ms": steps,
+                          "ms_steps_1_3": ms, "gflops": 2.0 * prods / (ms * 1e-3) / 1e9, "reps": reps}), flush=True)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--time":
+        time_reference()
+        return
     out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__))
     os.makedirs(out_dir, exist_ok=True)
     d = Driver()

@@ -183,6 +183,9 @@ def test_galerkin_128_whole_product(handle, galerkin128, algo, sizing):
 
 
 def test_er_batch_512(handle):
+    """All 512 problems of the batch configuration in one batched product:
+    every 16th problem checked in full (tile count from the oracle's step 1,
+    every entry against the FP64 Gustavson), the product count of all."""
     pairs = synth.er_batch(512)
     bt = api.Batch(handle, pairs)
     bt.tune()
@@ -191,11 +194,12 @@ def test_er_batch_512(handle):
     for p in range(0, 512, 16):
         a, b = pairs[p]
         got = bt.result(p)
-        S = oracle.spgemm_tiles(a, b)
-        assert got["numtileC"] == S["numtileC"] and got["nnzC"] == S["nnzC"], p
-        for k in STRUCT_KEYS:
-            np.testing.assert_array_equal(got[k], S[k].astype(got[k].dtype), err_msg=f"{p}:{k}")
-        assert rel(got["tile_valC"], S["tile_valC"]) <= TOL32, p
+        assert got["numtileC"] == oracle_counts(a, b)["numtileC"], p
+        d = dict(tile_ptr=got["tile_ptrC"].astype(np.int64), tile_colidxC=got["tile_colidxC"],
+                 tile_nnzC=got["tile_nnzC"], maskC=got["maskC"], ptrRowC=got["ptrRowC"], tile_colC=got["tile_colC"],
+                 tile_valC=got["tile_valC"])
+        r = oracle.check_tilerows(a, b, 0, (a.m + 15) // 16, d)
+        assert r["mismatches"] == 0 and r["rel_frob"] <= TOL32, (p, r)
     bt.free()
 
 
