@@ -5,7 +5,9 @@
 // for B's CSC tile order.  The reference does this on one host thread with
 // std::sort per tile-row; here every tile-row is a thread block:
 //
-//   tiler_count   tile-row CTA, shared-memory bitmap over tile columns -> #tiles
+//   tiler_class   tile-rows classed: empty, narrow (one warp each), wide (one
+//                 thread block each)
+//   tiler_count   shared-memory bitmap over tile columns -> #tiles
 //   (scan)        tile_ptr
 //   tiler_fill    rebuild bitmap, word-prefix ranks -> sorted tile_columnidx;
 //                 per nonzero: tile index by rank, position inside its
@@ -29,19 +31,196 @@ constexpr int TL_MAX_WORDS = 16384;  // tilen <= 524288 (n <= 8,388,608)
 
 __device__ __forceinline__ uint16_t colbit(int c) { return (uint16_t)(0x8000u >> (c & 15)); }
 
+// Tile-rows are classed once per tiling: an empty one gets its count of 0
+// here; a narrow one (at most TL_NARROW_NNZ nonzeros over at most
+// TL_NARROW_WORDS bitmap words of tile columns -- stencils, aggregation
+// operators) is tiled by one warp; the rest (power-law rows spanning the
+// matrix) by one thread block each.  The lists are unordered: counts and
+// positions come from the tile-row index.
+constexpr int TL_NARROW_WORDS = 128;
+constexpr int TL_NARROW_NNZ = 4096;
+
+__global__ void tiler_class_kernel(int tilem, int m, const int* __restrict__ rp, const int* __restrict__ ci,
+                                   int* __restrict__ tile_cnt, int* __restrict__ narrow, int* __restrict__ wide,
+                                   int* __restrict__ n_lists) {
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x; i0 < tilem; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + (int)threadIdx.x;
+        int cls = -1;  // -1 none, 0 narrow, 1 wide
+        if (i < tilem) {
+            const int r0 = i * TS, r1 = min(r0 + TS, m);
+            if (rp[r0] == rp[r1]) {
+                tile_cnt[i] = 0;
+            } else {
+                int lo = 0x7fffffff, hi = -1;
+                for (int r = r0; r < r1; r++) {
+                    const int s = rp[r], e = rp[r + 1];
+                    if (e > s) { lo = min(lo, ci[s]); hi = max(hi, ci[e - 1]); }
+                }
+                // columns outside [0, n) or out of order are caught by the count passes
+                const int nwd = (max(hi, 0) >> 9) - (max(lo, 0) >> 9) + 1;
+                cls = (rp[r1] - rp[r0] <= TL_NARROW_NNZ && nwd <= TL_NARROW_WORDS && lo >= 0) ? 0 : 1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            const unsigned b = __ballot_sync(0xffffffffu, cls == c);
+            int base = 0;
+            if (lane == 0 && b) base = atomicAdd(&n_lists[c], __popc(b));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (cls == c) (c ? wide : narrow)[base + __popc(b & lanemask_lt())] = i;
+        }
+    }
+}
+
+// Start word (tile column / 32) of a narrow tile-row: the smallest first
+// column of its rows, reduced across the warp (lanes < 16 hold a row each).
+__device__ __forceinline__ int narrow_wlo(int r0, int r1, const int* __restrict__ rp, const int* __restrict__ ci) {
+    const int lane = threadIdx.x & 31;
+    int lo = 0x7fffffff;
+    if (lane < r1 - r0) {
+        const int s = rp[r0 + lane], e = rp[r0 + lane + 1];
+        if (e > s) lo = ci[s];
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, d));
+    return max(lo, 0) >> 9;
+}
+
+// One warp per narrow tile-row: its tile columns in a per-warp bitmap of
+// TL_NARROW_WORDS words (validating canonical CSR on the way), the count.
+__global__ void __launch_bounds__(TL_THREADS)
+tiler_count_narrow_kernel(int m, int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                          const int* __restrict__ rows, const int* __restrict__ n_rows, int* __restrict__ tile_cnt,
+                          unsigned* flags) {
+    __shared__ uint32_t s_bm[TL_WARPS][TL_NARROW_WORDS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* bm = s_bm[warp];
+    const int nr = *n_rows;
+    for (int idx = blockIdx.x * TL_WARPS + warp; idx < nr; idx += gridDim.x * TL_WARPS) {
+        const int i = rows[idx];
+        const int r0 = i * TS, r1 = min(r0 + TS, m);
+        const int wlo = narrow_wlo(r0, r1, rp, ci);
+        for (int w = lane; w < TL_NARROW_WORDS; w += 32) bm[w] = 0u;
+        __syncwarp();
+        for (int r = r0; r < r1; r++) {
+            const int s = rp[r], e = rp[r + 1];
+            for (int j = s + lane; j < e; j += 32) {
+                const int c = ci[j];
+                const int prev = (j > s) ? ci[j - 1] : -1;
+                if (c < 0 || c >= n || (j > s && prev >= c)) {
+                    atomicOr(flags, DERR_NONCANONICAL);
+                    continue;
+                }
+                const int tc = c >> 4;
+                if (j > s && (prev >> 4) == tc) continue;  // segment already marked
+                const int w = (tc >> 5) - wlo;
+                if (w < 0 || w >= TL_NARROW_WORDS) { atomicOr(flags, DERR_NONCANONICAL); continue; }
+                atomicOr(&bm[w], 1u << (tc & 31));
+            }
+        }
+        __syncwarp();
+        int cnt = 0;
+        for (int w = lane; w < TL_NARROW_WORDS; w += 32) cnt += __popc(bm[w]);
+        cnt = warp_sum(cnt);
+        if (lane == 0) tile_cnt[i] = cnt;
+        __syncwarp();
+    }
+}
+
+// One warp per narrow tile-row: sorted tile columns, and per nonzero its
+// tile and its position in its (row, tile) segment; segment heads write the
+// row count and row mask (tiler_fill_kernel's work for one tile-row).
+__global__ void __launch_bounds__(TL_THREADS)
+tiler_fill_narrow_kernel(int m, const int* __restrict__ rp, const int* __restrict__ ci,
+                         const int* __restrict__ rows, const int* __restrict__ n_rows,
+                         const int* __restrict__ tile_ptr, int* __restrict__ tile_columnidx,
+                         int* __restrict__ tile_rowof, uint8_t* __restrict__ row_cnt, uint16_t* __restrict__ mask,
+                         int* __restrict__ tmp_t, uint8_t* __restrict__ tmp_rp) {
+    __shared__ uint32_t s_bm[TL_WARPS][TL_NARROW_WORDS];
+    __shared__ uint32_t s_pre[TL_WARPS][TL_NARROW_WORDS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* bm = s_bm[warp];
+    uint32_t* pre = s_pre[warp];
+    constexpr int WPL = TL_NARROW_WORDS / 32;  // words per lane, contiguous
+    const int nr = *n_rows;
+    for (int idx = blockIdx.x * TL_WARPS + warp; idx < nr; idx += gridDim.x * TL_WARPS) {
+        const int i = rows[idx];
+        const int r0 = i * TS, r1 = min(r0 + TS, m);
+        const int wlo = narrow_wlo(r0, r1, rp, ci);
+        for (int w = lane; w < TL_NARROW_WORDS; w += 32) bm[w] = 0u;
+        __syncwarp();
+        for (int r = r0; r < r1; r++) {
+            const int s = rp[r], e = rp[r + 1];
+            for (int j = s + lane; j < e; j += 32) {
+                const int tc = ci[j] >> 4;
+                if (j > s && (ci[j - 1] >> 4) == tc) continue;
+                atomicOr(&bm[(tc >> 5) - wlo], 1u << (tc & 31));
+            }
+        }
+        __syncwarp();
+        // exclusive popcount prefix of the words, WPL contiguous words a lane
+        uint32_t local = 0;
+#pragma unroll
+        for (int q = 0; q < WPL; q++) local += __popc(bm[lane * WPL + q]);
+        const uint32_t inc = warp_incl_scan(local, (unsigned)lane);
+        uint32_t run = inc - local;
+        const int tbase = tile_ptr[i];
+#pragma unroll
+        for (int q = 0; q < WPL; q++) {
+            const int w = lane * WPL + q;
+            uint32_t bits = bm[w];
+            pre[w] = run;
+            int pos = tbase + (int)run;
+            run += __popc(bits);
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                tile_columnidx[pos] = (wlo + w) * 32 + b;
+                if (tile_rowof) tile_rowof[pos] = i;
+                pos++;
+                bits &= bits - 1u;
+            }
+        }
+        __syncwarp();
+        for (int r = r0; r < r1; r++) {
+            const int s = rp[r], e = rp[r + 1], rl = r - r0;
+            for (int j = s + lane; j < e; j += 32) {
+                const int c = ci[j], tc = c >> 4;
+                const int w = (tc >> 5) - wlo;
+                const int t = tbase + (int)pre[w] + __popc(bm[w] & ((1u << (tc & 31)) - 1u));
+                int p = 0;
+                for (int q = j - 1; q >= s && (ci[q] >> 4) == tc; q--) p++;
+                tmp_t[j] = t;
+                tmp_rp[j] = (uint8_t)((rl << 4) | p);
+                if (p == 0) {
+                    int len = 1;
+                    uint16_t mk = colbit(c);
+                    for (int q = j + 1; q < e && (ci[q] >> 4) == tc; q++) {
+                        len++;
+                        mk |= colbit(ci[q]);
+                    }
+                    row_cnt[(int64_t)t * TS + rl] = (uint8_t)len;
+                    mask[(int64_t)t * TS + rl] = mk;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// One thread block per wide tile-row (persistent over the list of them).
 __global__ void __launch_bounds__(TL_THREADS)
 tiler_count_kernel(int m, int n, int nwords, const int* __restrict__ rp, const int* __restrict__ ci,
-                   int* __restrict__ tile_cnt, unsigned* flags) {
+                   const int* __restrict__ rows, const int* __restrict__ n_rows, int* __restrict__ tile_cnt,
+                   unsigned* flags) {
     extern __shared__ uint32_t bm[];
     __shared__ int s_red[TL_WARPS];
-    const int i = blockIdx.x;
-    const int r0 = i * TS, r1 = min(r0 + TS, m);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (rp[r0] == rp[r1]) {
-        if (threadIdx.x == 0) tile_cnt[i] = 0;
-        return;
-    }
     __shared__ int s_span[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nr = *n_rows;
+    for (int idx = blockIdx.x; idx < nr; idx += gridDim.x) {
+    const int i = rows[idx];
+    const int r0 = i * TS, r1 = min(r0 + TS, m);
     if (threadIdx.x == 0) { s_span[0] = 0x7fffffff; s_span[1] = -1; }
     __syncthreads();
     if (threadIdx.x < (unsigned)(r1 - r0)) {
@@ -84,6 +263,8 @@ tiler_count_kernel(int m, int n, int nwords, const int* __restrict__ rp, const i
         int t = 0;
         for (int w = 0; w < TL_WARPS; w++) t += s_red[w];
         tile_cnt[i] = t;
+    }
+    __syncthreads();
     }
 }
 
@@ -137,6 +318,7 @@ __device__ __forceinline__ int rank_of(const uint32_t* bm, const uint32_t* pre, 
 
 __global__ void __launch_bounds__(TL_THREADS)
 tiler_fill_kernel(int m, int nwords, const int* __restrict__ rp, const int* __restrict__ ci,
+                  const int* __restrict__ rows, const int* __restrict__ n_rows,
                   const int* __restrict__ tile_ptr, int* __restrict__ tile_columnidx,
                   int* __restrict__ tile_rowof, uint8_t* __restrict__ row_cnt,
                   uint16_t* __restrict__ mask, int* __restrict__ tmp_t, uint8_t* __restrict__ tmp_rp) {
@@ -145,10 +327,11 @@ tiler_fill_kernel(int m, int nwords, const int* __restrict__ rp, const int* __re
     uint32_t* pre = sm + nwords;
     __shared__ int64_t s_sh[TL_WARPS + 1];
     __shared__ int s_span[4];
-    const int i = blockIdx.x;
-    const int r0 = i * TS, r1 = min(r0 + TS, m);
-    if (rp[r0] == rp[r1]) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nr = *n_rows;
+    for (int idx = blockIdx.x; idx < nr; idx += gridDim.x) {
+    const int i = rows[idx];
+    const int r0 = i * TS, r1 = min(r0 + TS, m);
     build_rank_table(i, m, rp, ci, bm, pre, s_sh, s_span);
     const int wlo = s_span[2], nwd = s_span[3];
     const int tbase = tile_ptr[i];
@@ -189,6 +372,8 @@ tiler_fill_kernel(int m, int nwords, const int* __restrict__ rp, const int* __re
                 mask[(int64_t)t * TS + rl] = mk;
             }
         }
+    }
+    __syncthreads();
     }
 }
 
@@ -348,17 +533,32 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
     const int* rp = out->row_ptr;
     const int* ci = out->col_idx;
 
-    // pass 1: tiles per tile-row
+    // pass 1: tiles per tile-row (narrow tile-rows one warp each, wide ones
+    // one thread block each)
     ScratchList sc(h);
     int* tile_cnt_rows = nullptr;
+    int *narrow = nullptr, *wide = nullptr, *n_lists = nullptr;
     SPG_TRY(sc.alloc(&tile_cnt_rows, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&narrow, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&wide, (size_t)tilem + 1));
+    SPG_TRY(sc.alloc(&n_lists, 2));
     SPG_TRY(spg_alloc_t(h, &out->tile_ptr, (size_t)tilem + 1));
     const size_t smem1 = sizeof(uint32_t) * nwords;
     const size_t smem2 = 2 * sizeof(uint32_t) * nwords;
     SPG_CUDA(h, cudaFuncSetAttribute(tiler_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
     SPG_CUDA(h, cudaFuncSetAttribute(tiler_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+    SPG_CUDA(h, cudaMemsetAsync(n_lists, 0, 2 * sizeof(int), h->stream));
+    const int grid_rows = grid_for(h, (int64_t)tilem * 32, TL_THREADS);  // a warp per tile-row, capped
+    const int grid_wide = h->num_sms * 8;  // persistent blocks over the wide tile-rows
     if (tilem > 0) {
-        tiler_count_kernel<<<tilem, TL_THREADS, smem1, h->stream>>>(m, n, nwords, rp, ci, tile_cnt_rows, h->d_flags);
+        tiler_class_kernel<<<grid_for(h, tilem, 256), 256, 0, h->stream>>>(tilem, m, rp, ci, tile_cnt_rows, narrow,
+                                                                          wide, n_lists);
+        SPG_LAUNCHED(h);
+        tiler_count_narrow_kernel<<<grid_rows, TL_THREADS, 0, h->stream>>>(m, n, rp, ci, narrow, n_lists,
+                                                                           tile_cnt_rows, h->d_flags);
+        SPG_LAUNCHED(h);
+        tiler_count_kernel<<<grid_wide, TL_THREADS, smem1, h->stream>>>(m, n, nwords, rp, ci, wide, n_lists + 1,
+                                                                        tile_cnt_rows, h->d_flags);
         SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i32(h, tile_cnt_rows, out->tile_ptr, tilem));
@@ -384,9 +584,13 @@ spg_status spg_build_tiles(spg_handle_t h, int m, int n, int64_t nnz, const int*
     SPG_CUDA(h, cudaMemsetAsync(ptr_row, 0, (size_t)numtile * TS, h->stream));
     SPG_CUDA(h, cudaMemsetAsync(mask_row, 0, sizeof(uint16_t) * (size_t)numtile * TS, h->stream));
     if (tilem > 0) {
-        tiler_fill_kernel<<<tilem, TL_THREADS, smem2, h->stream>>>(m, nwords, rp, ci, out->tile_ptr,
-                                                                   out->tile_columnidx, tile_rowof, ptr_row,
-                                                                   mask_row, tmp_t, tmp_rp);
+        tiler_fill_narrow_kernel<<<grid_rows, TL_THREADS, 0, h->stream>>>(m, rp, ci, narrow, n_lists, out->tile_ptr,
+                                                                          out->tile_columnidx, tile_rowof, ptr_row,
+                                                                          mask_row, tmp_t, tmp_rp);
+        SPG_LAUNCHED(h);
+        tiler_fill_kernel<<<grid_wide, TL_THREADS, smem2, h->stream>>>(m, nwords, rp, ci, wide, n_lists + 1,
+                                                                       out->tile_ptr, out->tile_columnidx, tile_rowof,
+                                                                       ptr_row, mask_row, tmp_t, tmp_rp);
         SPG_LAUNCHED(h);
     }
     if (numtile > 0) {
