@@ -326,9 +326,28 @@ __device__ __forceinline__ int segment_end(Cols col, int p0, int be, int g, int 
 // per round with all their loads in flight: consecutive lanes read
 // consecutive B entries of one segment, and a slow search stalls only its
 // own warp.  The caller synchronises the block afterwards.
+// In the numeric walk, segments of at least LQ_MIN products are not swept by
+// the warp that found them: they wait in a block queue of LQ_CAP entries that
+// every warp drains together once the walk is over (drain_long).  A hub B row
+// can hold thousands of products inside one window; swept by one warp, it
+// kept the other warps waiting at the window's barrier (R-MAT 2^20 numeric
+// 224 -> 218 ms).
+constexpr int LQ_CAP = 128;
+constexpr int LQ_MIN = 256;
+
+template <typename Entry>
+struct LongQueue {
+    int n;                 // segments offered (may pass LQ_CAP: the rest stayed with their warp)
+    int next;              // drain ticket, in products
+    int p0[LQ_CAP];        // first B position
+    int pre[LQ_CAP + 1];   // exclusive prefix of the lengths (filled by drain_long)
+    int r[LQ_CAP];         // the A nonzero's row in its tile
+    Entry e[LQ_CAP];
+};
+
 template <typename Op, typename Cols>
 __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, const int* s_rows, int limit, Cols col,
-                                            int* s_fx, Op op) {
+                                            int* s_fx, Op op, LongQueue<typename Op::Entry>* lq) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     while (true) {
@@ -361,6 +380,16 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
             cu.pos[x] = hi;
             cu.col[x] = nc;
             cu.len[x] = len;
+            if (lq && len >= LQ_MIN) {  // leave it to the whole block
+                const int k = atomicAdd(&lq->n, 1);
+                if (k < LQ_CAP) {
+                    lq->p0[k] = p0;
+                    lq->pre[k] = len;
+                    lq->r[k] = r;
+                    lq->e[k] = ent;
+                    len = 0;
+                }
+            }
         }
         int inc = len;
 #pragma unroll
@@ -398,6 +427,76 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
                 if (pp[u] >= 0) op.apply(rr[u], cc[u], ee[u], ld[u]);
         }
     }
+}
+
+// Sweeps the queued long segments with every warp of the block: the lengths
+// become an exclusive prefix, then warps take 32 * SWU products at a time
+// from a ticket and find each product's segment by bisection of the prefix.
+// Called by all threads after the block's walk (a barrier ahead of it); the
+// caller synchronises afterwards.  Resets the queue.
+template <typename Op, typename Cols>
+__device__ __forceinline__ void drain_long(LongQueue<typename Op::Entry>* lq, Cols col, Op op) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nq = min(lq->n, LQ_CAP);
+    if (nq == 0) return;  // uniform: every thread read the same count after the barrier
+    if (warp == 0) {  // lengths -> exclusive prefix, LQ_CAP / 32 entries a lane
+        constexpr int PL = LQ_CAP / 32;
+        int v[PL], run = 0;
+#pragma unroll
+        for (int k = 0; k < PL; k++) {
+            const int i = lane * PL + k;
+            v[k] = i < nq ? lq->pre[i] : 0;
+            run += v[k];
+        }
+        int inc = run;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(FULL, inc, d);
+            if (lane >= d) inc += o;
+        }
+        int ex = inc - run;
+#pragma unroll
+        for (int k = 0; k < PL; k++) {
+            lq->pre[lane * PL + k] = ex;
+            ex += v[k];
+        }
+        if (lane == 31) lq->pre[LQ_CAP] = inc;
+        if (lane == 0) lq->next = 0;
+    }
+    __syncthreads();
+    const int total = lq->pre[LQ_CAP];
+    while (true) {
+        int q0 = 0;
+        if (lane == 0) q0 = atomicAdd(&lq->next, 32 * SWU);
+        q0 = __shfl_sync(FULL, q0, 0);
+        if (q0 >= total) break;
+        int pp[SWU], rr[SWU];
+        typename Op::Entry ee[SWU];
+#pragma unroll
+        for (int u = 0; u < SWU; u++) {
+            const int q = q0 + u * 32 + lane;
+            pp[u] = -1;
+            if (q < total) {
+                int lo = 0, hi = nq;  // last segment with pre <= q
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (lq->pre[mid] <= q) lo = mid; else hi = mid;
+                }
+                pp[u] = lq->p0[lo] + (q - lq->pre[lo]);
+                rr[u] = lq->r[lo];
+                ee[u] = lq->e[lo];
+            }
+        }
+        typename Op::Loaded ld[SWU];
+        int cc[SWU];
+#pragma unroll
+        for (int u = 0; u < SWU; u++) op.fetch(pp[u], &cc[u], &ld[u]);
+#pragma unroll
+        for (int u = 0; u < SWU; u++)
+            if (pp[u] >= 0) op.apply(rr[u], cc[u], ee[u], ld[u]);
+    }
+    (void)col;
 }
 
 // The walk's operations: entry(x) once per active nonzero (passed between
@@ -498,7 +597,10 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             }
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, w0, nt, wlo, nwd, bp, s_sh);
-            walk_window(it, cu, s_rows, limit, ColArray{b_ci}, &s_fx, SymOp{bp, wlo, masks32, b_ci});
+            // (one atomicOr a product: long segments cost their warp little,
+            // and a queue's two barriers cost more than it saved)
+            walk_window(it, cu, s_rows, limit, ColArray{b_ci}, &s_fx, SymOp{bp, wlo, masks32, b_ci},
+                        static_cast<LongQueue<SymOp::Entry>*>(nullptr));
             __syncthreads();
             // write-out: lane pair (2j, 2j+1) takes one tile, each lane 8 of its
             // rows, so a warp's stores cover 16 tiles' contiguous masks (512 B)
@@ -564,7 +666,9 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
     __shared__ int s_nt, s_fx, s_nrow;
+    __shared__ LongQueue<typename NumOp<V, ACC>::Entry> s_lq;
     const int tid = threadIdx.x;
+    if (tid == 0) s_lq.n = 0;
 
     while (next_item(ticket, item_prefix, tilem, item_lo, item_hi, tile_ptrC, a_rp, m, &s_it, s_rows,
                      band_rev ? nbands : 0, band_end)) {
@@ -654,9 +758,12 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
             for (int x = tid; x < nv; x += RW_THREADS) acc[x] = ACC(0);
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bp, s_sh);
-            walk_window(it, cu, s_rows, limit, ColEntries<V>{bcv}, &s_fx,
-                        NumOp<V, ACC>{bp, wlo, tinfo, rows, acc, a_val, bcv, it.e0});
+            const NumOp<V, ACC> nop{bp, wlo, tinfo, rows, acc, a_val, bcv, it.e0};
+            walk_window(it, cu, s_rows, limit, ColEntries<V>{bcv}, &s_fx, nop, &s_lq);
             __syncthreads();
+            drain_long(&s_lq, ColEntries<V>{bcv}, nop);
+            __syncthreads();
+            if (tid == 0) s_lq.n = 0;
             // column bytes: one thread per non-empty tile row writes its run;
             // values leave coalesced
             const int nrow = s_nrow;
