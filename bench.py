@@ -77,6 +77,10 @@ def workload(name: str) -> dict:
     if name == "stencil27f64":  # the reference's value type, for the comparison with its own kernels
         a = synth.stencil27_dof3(64, dtype=np.float64)
         return dict(kind="product", a=a, b=a, desc="C=A*A, A=27-point stencil 64^3 x 3 dof, FP64 N(0,1)")
+    if name.startswith("stencil27_"):  # smaller grids of the same stencil (profiling cases)
+        g = int(name[10:])
+        a = synth.stencil27_dof3(g)
+        return dict(kind="product", a=a, b=a, desc=f"C=A*A, A=27-point stencil {g}^3 x 3 dof, FP32 N(0,1)")
     if name == "mixed":
         a = synth.block_diag(synth.stencil27_dof3(40), synth.rmat(18, 16))
         return dict(kind="product", a=a, b=a, desc="C=A*A, A=block diagonal of a 27-point stencil 40^3 x 3 dof "

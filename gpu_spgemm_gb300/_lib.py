@@ -47,7 +47,8 @@ class SpgCTiles(C.Structure):
 class SpgStats(C.Structure):
     _fields_ = [("ms_step1", C.c_float), ("ms_step2", C.c_float), ("ms_step3", C.c_float),
                 ("products", I64), ("overflow_reruns", I64), ("work_items", I64), ("tensor_pairs", I64),
-                ("fp64_tiles", I64), ("algo_used", I32), ("sizing_fallbacks", I32), ("predicted_tiles", I64)]
+                ("fp64_tiles", I64), ("algo_used", I32), ("sizing_fallbacks", I32), ("predicted_tiles", I64),
+                ("numeric_algo", I32), ("reserved", I32)]
 
 
 # spg_band_fn: (user, band, row_begin, row_end)

@@ -836,8 +836,10 @@ size_t num_smem() {
 // plain 982 ms; 27-point x 3 dof (50 nnz/tile) plain 19 ms vs row-wise 45 ms.
 bool rowwise_fits(spg_handle_t h, const spg_tiles* B) {
     const int nwords_b = (B->tilen + 31) / 32;
-    return sym_smem(nwords_b) <= h->smem_optin && num_smem<double>() <= h->smem_optin;
+    return sym_smem(nwords_b) <= h->smem_optin && rowwise_numeric_fits(h);
 }
+
+bool rowwise_numeric_fits(spg_handle_t h) { return num_smem<double>() <= h->smem_optin; }
 
 static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                              RowwisePriv* rp) {

@@ -12,7 +12,12 @@ struct RowwisePriv {
     int grid = 0;
 };
 
+// Whether the row-wise kernels can run this product (shared memory for the
+// symbolic windows over B's tile columns, and for the numeric arena).
 bool rowwise_fits(spg_handle_t h, const spg_tiles* B);
+// Whether the row-wise numeric kernel can run (any B: its windows carry
+// their own rank bitmaps).
+bool rowwise_numeric_fits(spg_handle_t h);
 // skip_rows (optional, tilem flags): tile-rows whose work items are skipped
 // (the binned algorithm leaves them to the plain kernels).
 spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,

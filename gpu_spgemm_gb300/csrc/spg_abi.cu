@@ -560,10 +560,22 @@ extern "C" spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, con
 // or plain with dense pairs on the tensor cores.
 enum class NumPath { ROWWISE, PLAIN, MIXED, BINNED };
 
+// Tile pairs from which a product of FP64 data runs its numeric phase on the
+// row-wise kernels whatever its symbolic phase was.  GB300 executes FP64 at
+// 1/64 of its FP32 rate; the plain register kernel issues one FMA for each of
+// a B row's 16 columns per A entry (masked where the row has no entry), the
+// row-wise sweep one per product.  27-point stencil 64^3 x 3 dof, FP64: numeric
+// 87.4 ms plain, 36.3 ms row-wise.  Below this size the row-wise launch's
+// fixed costs lose (2-D Poisson 256^2: 0.18 ms plain, 0.27 ms row-wise).
+constexpr int64_t F64_ROWWISE_MIN_PAIRS = 1 << 20;
+
 // Checks that C is ready for step 3 (symbolic structure and masks) and picks
 // its path: MIXED for SPG_PREC_MIXED on FP32 data; ROWWISE when C's structure
-// came from the row-wise symbolic phase (or FP64 accumulation of FP32 data is
-// asked for); PLAIN otherwise.
+// came from the row-wise symbolic phase, when FP64 accumulation of FP32 data
+// is asked for, or (AUTO) for FP64 data from F64_ROWWISE_MIN_PAIRS tile
+// pairs; BINNED for a binned C; PLAIN otherwise.  The row-wise kernels build
+// their plan (work items per tile-row) on first use when the symbolic phase
+// did not.
 static spg_status numeric_path(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                                spg_precision prec, const spg_ctiles* C, NumPath* path) {
     SPG_TRY(validate_pair(h, A, B, C));
@@ -571,23 +583,30 @@ static spg_status numeric_path(spg_handle_t h, const spg_tiles* A, const spg_til
     if (C->numtileC > 0 && (!C->maskC || !C->tile_nnzC || !C->tile_valC))
         return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
     const CPriv* cp = static_cast<const CPriv*>(C->priv);
-    if (algo == SPG_ALGO_AUTO) algo = cp->algo;
-    // the row-wise kernels need their plan, made by a row-wise or binned symbolic phase
-    const bool rw_plan = cp->algo == SPG_ALGO_ROWWISE || cp->algo == SPG_ALGO_BINNED;
-    if ((algo == SPG_ALGO_ROWWISE || algo == SPG_ALGO_BINNED) && !rw_plan) algo = SPG_ALGO_PLAIN;
-    if (algo == SPG_ALGO_BINNED && cp->algo != SPG_ALGO_BINNED) algo = cp->algo;
+    const bool rw_ok = rowwise_numeric_fits(h);
+    if (algo == SPG_ALGO_AUTO) {
+        algo = cp->algo;
+        if (A->dtype == SPG_F64 && prec != SPG_PREC_MIXED && C->pairs >= F64_ROWWISE_MIN_PAIRS && rw_ok)
+            algo = SPG_ALGO_ROWWISE;
+    }
+    if (algo == SPG_ALGO_BINNED && cp->algo != SPG_ALGO_BINNED) algo = cp->algo;  // the bins come from step 1
+    if (algo == SPG_ALGO_ROWWISE && !rw_ok) algo = SPG_ALGO_PLAIN;
     if (prec == SPG_PREC_MIXED && A->dtype == SPG_F32)
         *path = NumPath::MIXED;
-    else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32 && rw_plan))
+    else if (algo == SPG_ALGO_ROWWISE || (prec == SPG_PREC_F64 && A->dtype == SPG_F32 && rw_ok))
         *path = NumPath::ROWWISE;  // FP64 accumulation of FP32 data: the row-wise kernels, every tile-row
     else if (prec == SPG_PREC_F64 && A->dtype == SPG_F32)
         return spg_fail(h, SPG_ERR_UNSUPPORTED,
-                        "numeric: FP64 accumulation of FP32 data needs a row-wise or binned symbolic phase");
+                        "numeric: FP64 accumulation of FP32 data needs the row-wise kernels' shared memory");
     else if (algo == SPG_ALGO_BINNED)
         *path = NumPath::BINNED;
     else
         *path = NumPath::PLAIN;
     return SPG_OK;
+}
+
+static int32_t path_algo(NumPath p) {
+    return p == NumPath::ROWWISE ? SPG_ALGO_ROWWISE : p == NumPath::BINNED ? SPG_ALGO_BINNED : SPG_ALGO_PLAIN;
 }
 
 static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
@@ -597,6 +616,7 @@ static spg_status numeric_impl(spg_handle_t h, const spg_tiles* A, const spg_til
     if (r0 < 0 || r1 < r0 || r1 > C->tilem) return spg_fail(h, SPG_ERR_INVALID, "numeric: bad tile-row range");
     CPriv* cp = static_cast<CPriv*>(C->priv);
     const bool whole = r0 == 0 && r1 == C->tilem;
+    h->stats.numeric_algo = path_algo(path);
     SPG_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
     const bool mixed = path == NumPath::MIXED;
     if (path == NumPath::ROWWISE) {
@@ -656,6 +676,7 @@ extern "C" spg_status spg_numeric_bands(spg_handle_t h, const spg_tiles* A, cons
     NumPath path;
     SPG_TRY(numeric_path(h, A, B, algo, prec, C, &path));
     CPriv* cp = static_cast<CPriv*>(C->priv);
+    h->stats.numeric_algo = path_algo(path);
     if (path != NumPath::ROWWISE && path != NumPath::BINNED) {
         float ms = 0.f;
         for (int j = 0; j < nbands; j++) {
@@ -755,8 +776,10 @@ extern "C" spg_status spg_spgemm(spg_handle_t h, const spg_tiles* A, const spg_t
                                  spg_precision prec, spg_ctiles* C) {
     SPG_TRY(spg_symbolic(h, A, B, algo, C));
     spg_stats keep = h->stats;
-    spg_status s = spg_numeric(h, A, B, SPG_ALGO_AUTO, prec, C);
+    // an explicit PLAIN keeps the numeric phase on the plain kernels too
+    spg_status s = spg_numeric(h, A, B, algo == SPG_ALGO_PLAIN ? SPG_ALGO_PLAIN : SPG_ALGO_AUTO, prec, C);
     keep.ms_step3 = h->stats.ms_step3;
+    keep.numeric_algo = h->stats.numeric_algo;
     keep.tensor_pairs = h->stats.tensor_pairs;
     keep.fp64_tiles = h->stats.fp64_tiles;
     keep.work_items += h->stats.work_items;

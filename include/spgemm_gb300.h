@@ -142,6 +142,8 @@ typedef struct {
     int32_t algo_used;          /* spg_algo the symbolic phase ran             */
     int32_t sizing_fallbacks;   /* step 1 ran exact because the learned slots did not fit */
     int64_t predicted_tiles;    /* C tile capacity from the sizing model (0: none) */
+    int32_t numeric_algo;       /* spg_algo the numeric phase ran (PLAIN for mixed precision) */
+    int32_t reserved;
 } spg_stats;
 
 /* ---- handle ---------------------------------------------------------------
@@ -211,7 +213,11 @@ spg_status spg_symbolic_tiles(spg_handle_t h, const spg_tiles* A, const spg_tile
 spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C);
 
 /* Replaces step 3 (step3_numeric_kernel_v2, src/spgemm_raw_kernels_v2.cuh:10-139,
- * launched at src/spgemm_raw_v2.cu:228-238): fills tile_valC and tile_colC. */
+ * launched at src/spgemm_raw_v2.cu:228-238): fills tile_valC and tile_colC.
+ * algo AUTO follows C's symbolic phase, except that FP64 data from 2^20 tile
+ * pairs on runs the row-wise kernels over every tile-row (the plain kernel's
+ * masked 16-wide FMAs waste GB300's FP64 rate); SPG_PREC_F64 on FP32 data
+ * always runs the row-wise kernels.  stats.numeric_algo reports the choice. */
 spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                        spg_precision prec, spg_ctiles* C);
 

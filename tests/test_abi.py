@@ -59,6 +59,14 @@ def test_binding_struct_layout_matches_header():
     assert [f for f, _ in _lib.SpgTiles._fields_] == flat, (flat, fields)
 
 
+def test_stats_layout_matches_header():
+    from gpu_spgemm_gb300 import _lib
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "spgemm_gb300.h")).read(), flags=re.S)
+    body = src[src.index("typedef struct {\n    float ms_step1;"):src.index("} spg_stats;")]
+    names = re.findall(r"^\s*\w+\s+(\w+);", body, flags=re.M)
+    assert [f for f, _ in _lib.SpgStats._fields_] == names, names
+
+
 def test_missing_library_fails_loudly(tmp_path):
     from gpu_spgemm_gb300 import _lib
     with pytest.raises(RuntimeError):

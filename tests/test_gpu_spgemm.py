@@ -118,6 +118,22 @@ def test_rowwise_fp64_accumulation_of_fp32(handle, name, a):
     got, S = check_product(handle, a, a, "rowwise", np.float32, prec="f64")
 
 
+@pytest.mark.parametrize("algo", ["auto", "plain"])
+def test_fp64_numeric_on_rowwise_kernels(handle, algo):
+    """FP64 data from 2^20 tile pairs (27-point stencil 26^3 x 3 dof, 1.66 M
+    pairs): the symbolic phase stays on the plain kernels (dense tiles), the
+    numeric phase (AUTO) runs every tile-row on the row-wise kernels, whose
+    plan is built at numeric time.  Same structure, FP64 values."""
+    a = synth.stencil27_dof3(26)
+    got, S = check_product(handle, a, a, algo, np.float64)
+    st = handle.stats()
+    assert st["algo_used"] == 1
+    assert st["numeric_algo"] == (2 if algo == "auto" else 1)
+    # FP64 accumulation of FP32 data after a plain symbolic phase
+    got, S = check_product(handle, a.astype(np.float32), a.astype(np.float32), "plain", np.float32, prec="f64")
+    assert handle.stats()["numeric_algo"] == 2
+
+
 def test_host_range_copy_matches_full(handle):
     import ctypes as C
     from gpu_spgemm_gb300 import _lib as L
