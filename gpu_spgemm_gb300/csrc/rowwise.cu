@@ -335,6 +335,16 @@ __device__ __forceinline__ int segment_end(Cols col, int p0, int be, int g, int 
 constexpr int LQ_CAP = 128;
 constexpr int LQ_MIN = 256;
 
+// One entry of a warp's owner table: a segment that overlaps the products
+// of the current sweep round.  A flat product index q of the warp's step maps
+// to B position base + q.
+template <typename Entry>
+struct Owner {
+    int base;  // first B position of the segment minus its first flat index
+    int r;     // the A nonzero's row in its tile
+    Entry e;
+};
+
 template <typename Entry>
 struct LongQueue {
     int n;                 // segments offered (may pass LQ_CAP: the rest stayed with their warp)
@@ -347,7 +357,8 @@ struct LongQueue {
 
 template <typename Op, typename Cols>
 __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, const int* s_rows, int limit, Cols col,
-                                            int* s_fx, Op op, LongQueue<typename Op::Entry>* lq) {
+                                            int* s_fx, Op op, LongQueue<typename Op::Entry>* lq,
+                                            Owner<typename Op::Entry>* own) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     while (true) {
@@ -400,24 +411,36 @@ __device__ __forceinline__ void walk_window(const ItemInfo& it, Cursors cu, cons
         const int P = __shfl_sync(FULL, inc, 31);
         const int off = inc - len;  // exclusive offset of this lane's segment
         for (int q0 = 0; q0 < P; q0 += 32 * SWU) {
+            // the segments overlapping products [q0, q0 + 32 SWU), in lane
+            // order, go to the warp's owner table; each marks its first
+            // product in the round (the one carried in: the round's first) in
+            // SWU words of start bits.  A product's owner is the last segment
+            // starting at or before it: its index is the count of start bits
+            // up to the product's position, less one.
+            const bool ov = len > 0 && off < q0 + 32 * SWU && off + len > q0;
+            const int slot = max(off - q0, 0);
+            const unsigned ovm = __ballot_sync(FULL, ov);
+            if (ov) own[__popc(ovm & lanemask_lt())] = Owner<typename Op::Entry>{p0 - off, r, ent};
+            unsigned sb[SWU];
+#pragma unroll
+            for (int u = 0; u < SWU; u++)
+                sb[u] = __reduce_or_sync(FULL, (ov && (slot >> 5) == u) ? 1u << (slot & 31) : 0u);
+            __syncwarp();
             int pp[SWU], rr[SWU];
             typename Op::Entry ee[SWU];
+            int before = 0;  // start bits in the words of earlier u
 #pragma unroll
             for (int u = 0; u < SWU; u++) {
                 const int q = q0 + u * 32 + lane;
-                // owner: last lane j with off_j <= q (it has q < off_j + len_j)
-                int lo = 0, hi = 32;
-#pragma unroll
-                for (int s2 = 0; s2 < 5; s2++) {
-                    const int mid = (lo + hi) >> 1;
-                    const int om = __shfl_sync(FULL, off, mid);
-                    if (om <= q) lo = mid; else hi = mid;
-                }
-                const int jp0 = __shfl_sync(FULL, p0, lo), joff = __shfl_sync(FULL, off, lo);
-                rr[u] = __shfl_sync(FULL, r, lo);
-                ee[u] = op.shfl(ent, lo);
-                pp[u] = q < P ? jp0 + (q - joff) : -1;
+                // (2 << lane) - 1: positions 0..lane of this word (all 32 for lane 31)
+                const int k = before + __popc(sb[u] & ((2u << lane) - 1u)) - 1;  // >= 0: position q0 is covered
+                before += __popc(sb[u]);
+                const Owner<typename Op::Entry> o = own[k];
+                pp[u] = q < P ? o.base + q : -1;
+                rr[u] = o.r;
+                ee[u] = o.e;
             }
+            __syncwarp();  // every lane has read the table before the next round writes it
             typename Op::Loaded ld[SWU];
             int cc[SWU];
 #pragma unroll
@@ -499,8 +522,8 @@ __device__ __forceinline__ void drain_long(LongQueue<typename Op::Entry>* lq, Co
     (void)col;
 }
 
-// The walk's operations: entry(x) once per active nonzero (passed between
-// lanes by shfl), fetch(p) per product with the round's other loads (the B
+// The walk's operations: entry(x) once per active nonzero (handed to the
+// lanes sweeping its products through the owner table), fetch(p) per product with the round's other loads (the B
 // entry's column, and its value for the numeric product; p < 0: none), and
 // apply(r, c, entry, loaded).
 
@@ -513,7 +536,6 @@ struct SymOp {
     uint32_t* masks32;
     const int* b_ci;
     __device__ __forceinline__ Entry entry(int) const { return Entry{}; }
-    __device__ __forceinline__ Entry shfl(Entry, int) const { return Entry{}; }
     __device__ __forceinline__ void fetch(int p, int* c, Loaded*) const { *c = p >= 0 ? __ldg(&b_ci[p]) : 0; }
     __device__ __forceinline__ void apply(int r, int c, Entry, Loaded) const {
         const int idx = r * WS + wrank(bp, wlo, c >> 4);
@@ -538,9 +560,6 @@ struct NumOp {
     const BEntry<V>* bcv;
     int e0;
     __device__ __forceinline__ Entry entry(int x) const { return Entry{(ACC)__ldg(&a_val[e0 + x])}; }
-    __device__ __forceinline__ Entry shfl(Entry e, int src) const {
-        return Entry{__shfl_sync(0xffffffffu, e.va, src)};
-    }
     __device__ __forceinline__ void fetch(int p, int* c, Loaded* l) const {
         if (p >= 0) {
             const BEntry<V> e = bcv[p];
@@ -576,6 +595,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
     __shared__ int s_rows[TS + 1];
     __shared__ int64_t s_sh[RW_WARPS + 1];
     __shared__ int s_fx;
+    __shared__ Owner<SymOp::Entry> s_own[RW_THREADS];  // 32 entries per warp
     const int tid = threadIdx.x;
 
     while (next_item(ticket, item_prefix, tilem, 0, nitems, tile_ptrC, a_rp, m, &s_it, s_rows)) {
@@ -600,7 +620,7 @@ rw_symbolic_kernel(int m, int nwords_b, const int64_t* __restrict__ item_prefix,
             // (one atomicOr a product: long segments cost their warp little,
             // and a queue's two barriers cost more than it saved)
             walk_window(it, cu, s_rows, limit, ColArray{b_ci}, &s_fx, SymOp{bp, wlo, masks32, b_ci},
-                        static_cast<LongQueue<SymOp::Entry>*>(nullptr));
+                        static_cast<LongQueue<SymOp::Entry>*>(nullptr), s_own + (tid & ~31));
             __syncthreads();
             // write-out: lane pair (2j, 2j+1) takes one tile, each lane 8 of its
             // rows, so a warp's stores cover 16 tiles' contiguous masks (512 B)
@@ -667,6 +687,7 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
     __shared__ int64_t s_sh[RW_WARPS + 1];
     __shared__ int s_nt, s_fx, s_nrow;
     __shared__ LongQueue<typename NumOp<V, ACC>::Entry> s_lq;
+    __shared__ Owner<typename NumOp<V, ACC>::Entry> s_own[RW_THREADS];  // 32 entries per warp
     const int tid = threadIdx.x;
     if (tid == 0) s_lq.n = 0;
 
@@ -759,7 +780,7 @@ rw_numeric_kernel(int m, const int64_t* __restrict__ item_prefix, int tilem, int
             if (tid == 0) s_fx = 0;
             build_window_rank(colidxC, t0, ntw, wlo, nwd, bp, s_sh);
             const NumOp<V, ACC> nop{bp, wlo, tinfo, rows, acc, a_val, bcv, it.e0};
-            walk_window(it, cu, s_rows, limit, ColEntries<V>{bcv}, &s_fx, nop, &s_lq);
+            walk_window(it, cu, s_rows, limit, ColEntries<V>{bcv}, &s_fx, nop, &s_lq, s_own + (tid & ~31));
             __syncthreads();
             drain_long(&s_lq, ColEntries<V>{bcv}, nop);
             __syncthreads();
@@ -815,6 +836,11 @@ __global__ void band_plan_kernel(int nbands, const int* __restrict__ rows, const
     }
 }
 
+// Static shared memory of the kernels (owner tables, queue, item state) is
+// kept below this reserve: the dynamic sizes are checked against the opt-in
+// limit less it.
+constexpr size_t RW_STATIC_RESERVE = 12288;
+
 size_t sym_smem(int nwords_b) {
     return (size_t)WS * 8 * 4 + (size_t)MAXA_SMEM * 16 + (size_t)nwords_b * 8;
 }
@@ -836,10 +862,10 @@ size_t num_smem() {
 // plain 982 ms; 27-point x 3 dof (50 nnz/tile) plain 19 ms vs row-wise 45 ms.
 bool rowwise_fits(spg_handle_t h, const spg_tiles* B) {
     const int nwords_b = (B->tilen + 31) / 32;
-    return sym_smem(nwords_b) <= h->smem_optin && rowwise_numeric_fits(h);
+    return sym_smem(nwords_b) + RW_STATIC_RESERVE <= h->smem_optin && rowwise_numeric_fits(h);
 }
 
-bool rowwise_numeric_fits(spg_handle_t h) { return num_smem<double>() <= h->smem_optin; }
+bool rowwise_numeric_fits(spg_handle_t h) { return num_smem<double>() + RW_STATIC_RESERVE <= h->smem_optin; }
 
 static spg_status rw_prepare(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                              RowwisePriv* rp) {
@@ -886,7 +912,7 @@ spg_status rowwise_symbolic(spg_handle_t h, const spg_tiles* A, const spg_tiles*
     h->stats.work_items = rp->nitems;
     const int nwords_b = (B->tilen + 31) / 32;
     const size_t smem = sym_smem(nwords_b);
-    if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise symbolic: B too wide");
+    if (smem + RW_STATIC_RESERVE > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise symbolic: B too wide");
     SPG_CUDA(h, cudaFuncSetAttribute(rw_symbolic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SPG_CUDA(h, cudaMemsetAsync(rp->counters, 0, sizeof(unsigned long long), h->stream));
     int occ = 1;
@@ -914,7 +940,8 @@ template <typename V, typename ACC>
 static spg_status launch_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,
                                  RowwisePriv* rp, int64_t item_lo, int64_t item_hi, const BandArgs& ba) {
     size_t smem = num_smem<ACC>();
-    if (smem > h->smem_optin) return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: shared memory too small");
+    if (smem + RW_STATIC_RESERVE > h->smem_optin)
+        return spg_fail(h, SPG_ERR_UNSUPPORTED, "row-wise numeric: shared memory too small");
     // grow the arena into the shared memory left at the blocks per SM the
     // registers allow (two for FP32 accumulators, one for FP64); keep the
     // fixed size if the occupancy query disagrees
