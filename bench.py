@@ -50,9 +50,11 @@ TS = 16
 
 # DRAM traffic of the numeric kernel per algorithmic byte, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum of rw_numeric_kernel) on the
-# R-MAT 2^17 product, where the capture holds a few GB; the full-size launch's
-# traffic is this ratio times its algorithmic bytes.
-TRAFFIC_PER_ALGO_BYTE = {"rw_numeric_kernel": None}
+# R-MAT 2^17 product, where the capture holds a few GB: 2.881 + 2.418 GB
+# against 5.309 GB of algorithmic bytes.  A full-size launch's traffic is
+# reported as this ratio times its algorithmic bytes: a lower bound once B's
+# entries outgrow L2 (R-MAT 2^20: 134 MB).
+TRAFFIC_PER_ALGO_BYTE = {"rw_numeric_kernel": (2.880523e9 + 2.418124e9) / 5.308991570e9}
 
 # A tiles from which the bench attaches the learned sizing model (step 1's
 # slotted pass); the library's AUTO bins tile-rows from the same size on.
@@ -358,7 +360,7 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sized):
+def step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sized, numeric_algo=None):
     """Roofline of the dominant step's kernel: its algorithmic bytes (each
     array it must touch, read or written once) over its CUDA-event time."""
     hbm_peak, peak_src = load_peaks()
@@ -375,14 +377,18 @@ def step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sized):
     dom_bytes = {"step1": st1_bytes, "step2": sym_bytes, "step3": num_bytes}[dom]
     names = {"step1": "c1_slot_kernel + c1_compact_kernel" if sized else "c1_count_kernel + c1_fill_kernel",
              "step2": "rw_symbolic_kernel" if rowwise else "c2_symbolic_kernel",
-             "step3": "rw_numeric_kernel" if rowwise else "c3_numeric_kernel"}
+             "step3": {2: "rw_numeric_kernel", 3: "rw_numeric_kernel + c3_numeric_kernel (binned)"}.get(
+                 numeric_algo if numeric_algo is not None else (2 if rowwise else 1), "c3_numeric_kernel")}
+    if args.prec == "mixed" and names["step3"] == "c3_numeric_kernel":
+        names["step3"] = "c3_numeric_kernel + c3_tensor_kernel"
     achieved = dom_bytes / (steps_ms[dom] * 1e-3) / 1e9
     traffic = args.traffic
     traffic_src = "--traffic" if traffic is not None else None
-    ratio = TRAFFIC_PER_ALGO_BYTE.get(names[dom].split(" ")[0])
+    ratio = TRAFFIC_PER_ALGO_BYTE.get(names[dom])
     if traffic is None and ratio is not None:
         traffic = ratio * dom_bytes
-        traffic_src = "ncu DRAM bytes per algorithmic byte on the R-MAT 2^17 launch, times this launch's bytes"
+        traffic_src = ("ncu DRAM bytes per algorithmic byte of the R-MAT 2^17 launch (%.3f), times this launch's "
+                       "algorithmic bytes; a lower bound where B's entries exceed L2" % ratio)
     return {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_source": peak_src, "algorithmic_bytes": dom_bytes,
             "ms": steps_ms[dom], "traffic": traffic, "traffic_source": traffic_src}, a_b + b_b
@@ -505,7 +511,8 @@ def run_ours(args):
     s2 = statistics.mean(s["ms_step2"] for s in stats)
     s3 = statistics.mean(s["ms_step3"] for s in stats)
     rowwise = stats[-1].get("algo_used", 1) in (2, 3)
-    roofline, ab_bytes = step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sizing is not None)
+    roofline, ab_bytes = step_roofline(args, A, B, numtileC, nnzC, v, s1, s2, s3, rowwise, sizing is not None,
+                                       stats[-1].get("numeric_algo"))
     c_b = c_bytes(numtileC, nnzC, A.tilem, v)
 
     accuracy = None
