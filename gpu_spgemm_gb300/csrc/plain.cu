@@ -325,6 +325,14 @@ c3_numeric_kernel(int64_t ntiles, const int* __restrict__ tlist, const int* __re
                   unsigned* __restrict__ n_dense_tiles = nullptr) {
     const int lane = threadIdx.x & 31, r = lane & 15, hsel = lane >> 4;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    // FP64 accumulates in shared memory, one row of 16 per lane (padded rows:
+    // the 16 rows of a half-warp fall in distinct banks), and each A entry
+    // walks only its B row's set bits: GB300 issues FP64 at 1/64 of its FP32
+    // rate, and the register walk's 16 masked FMAs per A entry cost as much
+    // FP64 issue as a full B row.  FP32 keeps its registers.
+    constexpr bool SACC = sizeof(V) == 8;
+    __shared__ V s_acc[SACC ? 256 / 32 * 2 * TS * (TS + 1) : 1];
+    V* srow = s_acc + (SACC ? ((threadIdx.x >> 5) * 2 * TS + hsel * TS + r) * (TS + 1) : 0);
     for (int64_t idx = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < ntiles; idx += nwarps) {
         const int64_t t = LIST ? (int64_t)tlist[idx] : idx;  // the C tile (a listed one, or every one)
         const int64_t cbase = tile_nnzC[t];
@@ -332,6 +340,10 @@ c3_numeric_kernel(int64_t ntiles, const int* __restrict__ tlist, const int* __re
         V acc[TS];
 #pragma unroll
         for (int c = 0; c < TS; c++) acc[c] = V(0);
+        if (SACC) {
+#pragma unroll
+            for (int c = 0; c < TS; c++) srow[c] = V(0);
+        }
         bool skipped = false;  // warp-uniform: a dense pair was left to the tensor kernel
         auto do_pair = [&](int pa, int pb) {
             const int sA = __ldg(&a_tnnz[pa]), na = __ldg(&a_tnnz[pa + 1]) - sA;
@@ -347,11 +359,19 @@ c3_numeric_kernel(int64_t ntiles, const int* __restrict__ tlist, const int* __re
                 const V va = __ldg(&a_val[sA + e]);
                 const uint32_t mb = __ldg(&b_mask[(int64_t)pb * TS + kk]);
                 int off = sB + __ldg(&b_ptr16[(int64_t)pb * TS + kk]);
+                if (SACC) {
+                    for (uint32_t m = mb; m; off++) {  // set bits only, MSB-first (bit 15: column 0)
+                        const int c = __clz(m) - 16;
+                        m &= ~(0x8000u >> c);
+                        srow[c] = fma(va, __ldg(&b_val[off]), srow[c]);
+                    }
+                } else {
 #pragma unroll
-                for (int c = 0; c < TS; c++) {
-                    if (mb & (0x8000u >> c)) {
-                        acc[c] = fma(va, __ldg(&b_val[off]), acc[c]);
-                        off++;
+                    for (int c = 0; c < TS; c++) {
+                        if (mb & (0x8000u >> c)) {
+                            acc[c] = fma(va, __ldg(&b_val[off]), acc[c]);
+                            off++;
+                        }
                     }
                 }
             }
@@ -387,17 +407,32 @@ c3_numeric_kernel(int64_t ntiles, const int* __restrict__ tlist, const int* __re
                 }
             }
         }
-#pragma unroll
-        for (int c = 0; c < TS; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
-        if (hsel == 0) {
-            const uint32_t mc = maskC[t * TS + r];
-            int64_t p = cbase + ptrRowC[t * TS + r];
-#pragma unroll
-            for (int c = 0; c < TS; c++) {
-                if (mc & (0x8000u >> c)) {
-                    valC[p] = acc[c];
+        if (SACC) {
+            __syncwarp();  // both halves' rows are complete
+            if (hsel == 0) {
+                const V* other = srow + TS * (TS + 1);  // the same row of half 1
+                int64_t p = cbase + ptrRowC[t * TS + r];
+                for (uint32_t m = maskC[t * TS + r]; m; p++) {
+                    const int c = __clz(m) - 16;
+                    m &= ~(0x8000u >> c);
+                    valC[p] = srow[c] + other[c];
                     colC[p] = (uint8_t)((r << 4) | c);
-                    p++;
+                }
+            }
+            __syncwarp();  // half 1 clears its rows for the next tile only after the reads
+        } else {
+#pragma unroll
+            for (int c = 0; c < TS; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+            if (hsel == 0) {
+                const uint32_t mc = maskC[t * TS + r];
+                int64_t p = cbase + ptrRowC[t * TS + r];
+#pragma unroll
+                for (int c = 0; c < TS; c++) {
+                    if (mc & (0x8000u >> c)) {
+                        valC[p] = acc[c];
+                        colC[p] = (uint8_t)((r << 4) | c);
+                        p++;
+                    }
                 }
             }
         }

@@ -560,22 +560,12 @@ extern "C" spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, con
 // or plain with dense pairs on the tensor cores.
 enum class NumPath { ROWWISE, PLAIN, MIXED, BINNED };
 
-// Tile pairs from which a product of FP64 data runs its numeric phase on the
-// row-wise kernels whatever its symbolic phase was.  GB300 executes FP64 at
-// 1/64 of its FP32 rate; the plain register kernel issues one FMA for each of
-// a B row's 16 columns per A entry (masked where the row has no entry), the
-// row-wise sweep one per product.  27-point stencil 64^3 x 3 dof, FP64: numeric
-// 87.4 ms plain, 36.3 ms row-wise.  Below this size the row-wise launch's
-// fixed costs lose (2-D Poisson 256^2: 0.18 ms plain, 0.27 ms row-wise).
-constexpr int64_t F64_ROWWISE_MIN_PAIRS = 1 << 20;
-
 // Checks that C is ready for step 3 (symbolic structure and masks) and picks
 // its path: MIXED for SPG_PREC_MIXED on FP32 data; ROWWISE when C's structure
-// came from the row-wise symbolic phase, when FP64 accumulation of FP32 data
-// is asked for, or (AUTO) for FP64 data from F64_ROWWISE_MIN_PAIRS tile
-// pairs; BINNED for a binned C; PLAIN otherwise.  The row-wise kernels build
-// their plan (work items per tile-row) on first use when the symbolic phase
-// did not.
+// came from the row-wise symbolic phase, when it is asked for, or when FP64
+// accumulation of FP32 data is; BINNED for a binned C; PLAIN otherwise.  The
+// row-wise kernels build their plan (work items per tile-row) on first use
+// when the symbolic phase did not.
 static spg_status numeric_path(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                                spg_precision prec, const spg_ctiles* C, NumPath* path) {
     SPG_TRY(validate_pair(h, A, B, C));
@@ -584,11 +574,7 @@ static spg_status numeric_path(spg_handle_t h, const spg_tiles* A, const spg_til
         return spg_fail(h, SPG_ERR_INVALID, "numeric: C has no symbolic masks yet (spg_symbolic_masks)");
     const CPriv* cp = static_cast<const CPriv*>(C->priv);
     const bool rw_ok = rowwise_numeric_fits(h);
-    if (algo == SPG_ALGO_AUTO) {
-        algo = cp->algo;
-        if (A->dtype == SPG_F64 && prec != SPG_PREC_MIXED && C->pairs >= F64_ROWWISE_MIN_PAIRS && rw_ok)
-            algo = SPG_ALGO_ROWWISE;
-    }
+    if (algo == SPG_ALGO_AUTO) algo = cp->algo;
     if (algo == SPG_ALGO_BINNED && cp->algo != SPG_ALGO_BINNED) algo = cp->algo;  // the bins come from step 1
     if (algo == SPG_ALGO_ROWWISE && !rw_ok) algo = SPG_ALGO_PLAIN;
     if (prec == SPG_PREC_MIXED && A->dtype == SPG_F32)

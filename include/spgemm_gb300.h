@@ -214,10 +214,10 @@ spg_status spg_symbolic_masks(spg_handle_t h, const spg_tiles* A, const spg_tile
 
 /* Replaces step 3 (step3_numeric_kernel_v2, src/spgemm_raw_kernels_v2.cuh:10-139,
  * launched at src/spgemm_raw_v2.cu:228-238): fills tile_valC and tile_colC.
- * algo AUTO follows C's symbolic phase, except that FP64 data from 2^20 tile
- * pairs on runs the row-wise kernels over every tile-row (the plain kernel's
- * masked 16-wide FMAs waste GB300's FP64 rate); SPG_PREC_F64 on FP32 data
- * always runs the row-wise kernels.  stats.numeric_algo reports the choice. */
+ * algo AUTO follows C's symbolic phase; SPG_ALGO_ROWWISE runs the row-wise
+ * kernels on any C (their plan is built here when the symbolic phase did not
+ * build it), as does SPG_PREC_F64 on FP32 data.  stats.numeric_algo reports
+ * the choice. */
 spg_status spg_numeric(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_algo algo,
                        spg_precision prec, spg_ctiles* C);
 

@@ -118,20 +118,27 @@ def test_rowwise_fp64_accumulation_of_fp32(handle, name, a):
     got, S = check_product(handle, a, a, "rowwise", np.float32, prec="f64")
 
 
-@pytest.mark.parametrize("algo", ["auto", "plain"])
-def test_fp64_numeric_on_rowwise_kernels(handle, algo):
-    """FP64 data from 2^20 tile pairs (27-point stencil 26^3 x 3 dof, 1.66 M
-    pairs): the symbolic phase stays on the plain kernels (dense tiles), the
-    numeric phase (AUTO) runs every tile-row on the row-wise kernels, whose
-    plan is built at numeric time.  Same structure, FP64 values."""
-    a = synth.stencil27_dof3(26)
-    got, S = check_product(handle, a, a, algo, np.float64)
-    st = handle.stats()
-    assert st["algo_used"] == 1
-    assert st["numeric_algo"] == (2 if algo == "auto" else 1)
-    # FP64 accumulation of FP32 data after a plain symbolic phase
-    got, S = check_product(handle, a.astype(np.float32), a.astype(np.float32), "plain", np.float32, prec="f64")
-    assert handle.stats()["numeric_algo"] == 2
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_rowwise_numeric_after_plain_symbolic(handle, dtype):
+    """A C whose symbolic phase ran on the plain kernels (27-point stencil
+    26^3 x 3 dof) takes the row-wise numeric kernels when asked: their plan is
+    built at numeric time.  Same values as the plain numeric phase, and FP64
+    accumulation of FP32 data runs row-wise after a plain symbolic phase."""
+    a = synth.stencil27_dof3(26).astype(dtype)
+    S = oracle.spgemm_tiles(a, a)
+    A = api.csr2tile(handle, a)
+    B = api.build_csc_tiles(handle, a)
+    runs = [("auto", "f32", 1), ("rowwise", "f32", 2)] + ([("auto", "f64", 2)] if dtype == np.float32 else [])
+    for algo, prec, want in runs:
+        Cm = api.symbolic(handle, A, B, algo="plain")
+        api.numeric(handle, A, B, Cm, algo=algo, prec=prec)
+        assert handle.stats()["numeric_algo"] == want, (algo, prec)
+        got = Cm.to_host()
+        for k in STRUCT_KEYS:
+            np.testing.assert_array_equal(got[k], S[k].astype(got[k].dtype), err_msg=k)
+        tol = TOL[np.float64] if dtype == np.float64 else (1e-7 if prec == "f64" else TOL[np.float32])
+        assert rel_frob(got["tile_valC"], S["tile_valC"]) <= tol, (algo, prec)
+        Cm.free()
 
 
 def test_host_range_copy_matches_full(handle):
