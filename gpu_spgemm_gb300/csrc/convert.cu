@@ -225,7 +225,8 @@ extern "C" spg_status spg_galerkin(spg_handle_t h, int m, int nc, int64_t nnzA, 
     GTRY(spg_products(h, &tA, &tP, &prod1));
     GTRY(spg_spgemm(h, &tA, &tP, algo, prec, &AP));
     const spg_stats first = h->stats;
-    GTRY(ctiles_to_csr_impl(h, &AP, nullptr, nullptr, nullptr, &nnzAP));
+    nnzAP = AP.nnzC;  // known from the symbolic phase: one export pass, no counting pass
+    if (nnzAP >= 0x7fffffffLL) { s = spg_fail(h, SPG_ERR_INVALID, "galerkin: A*P does not fit an int32 CSR"); cleanup(); return s; }
     GTRY(spg_alloc_t(h, &ap_rp, (size_t)m + 1));
     GTRY(spg_alloc_t(h, &ap_ci, (size_t)nnzAP + 1));
     GTRY(spg_alloc(h, &ap_val, vs * ((size_t)nnzAP + 1)));

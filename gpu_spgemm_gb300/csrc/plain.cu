@@ -15,7 +15,7 @@ namespace {
 
 constexpr int C1_THREADS = 256;
 constexpr int C1_WARPS = C1_THREADS / 32;
-constexpr int SPEC_MAX = 32;  // pairs cached per C tile (MAX_MATCHED)
+constexpr int SPEC_MAX = SPEC_PAIRS_MAX;  // pairs cached per C tile (MAX_MATCHED)
 
 // Union of B's tile columns over A's tiles (i,k) as a bitmap.  The bitmap
 // covers only the tile-row's column span [jlo, jhi] (first / last tile column
@@ -716,6 +716,20 @@ __global__ void i64_to_i32_kernel(const int64_t* __restrict__ in, int* __restric
         out[t] = (int)in[t];
 }
 
+// C's tile count and step 1's tile pairs (C->pairs) in one round trip,
+// with step 1's device errors.
+spg_status read_tiles_and_pairs(spg_handle_t h, const int64_t* d_numtile, const unsigned long long* pairs_total,
+                                spg_ctiles* C, int64_t* numtileC) {
+    const int64_t* src[2] = {d_numtile, reinterpret_cast<const int64_t*>(pairs_total)};
+    int64_t v[2] = {0, 0};
+    SPG_TRY(spg_read_i64s_checked(h, 2, src, v, "symbolic step 1"));
+    if (v[0] > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "C has more than 2^31-1 tiles");
+    *numtileC = v[0];
+    C->numtileC = v[0];
+    C->pairs = v[1];
+    return SPG_OK;
+}
+
 int grid_cap(spg_handle_t h, int64_t units, int per_block, int per_sm) {
     int64_t g = ceil_div(units, per_block);
     const int64_t cap = (int64_t)h->num_sms * per_sm;
@@ -747,9 +761,7 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
     int64_t numtileC = 0;
-    SPG_TRY(spg_read_i64(h, ptr64 + tilem, &numtileC));
-    if (numtileC > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "C has more than 2^31-1 tiles");
-    C->numtileC = numtileC;
+    SPG_TRY(read_tiles_and_pairs(h, ptr64 + tilem, pairs_total, C, &numtileC));
     SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
     i64_to_i32_kernel<<<grid_cap(h, tilem + 1, 256, 8), 256, 0, h->stream>>>(ptr64, C->tile_ptrC, tilem + 1);
     SPG_LAUNCHED(h);
@@ -806,9 +818,7 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
     int64_t numtileC = 0;
-    SPG_TRY(spg_read_i64(h, ptr64 + tilem, &numtileC));
-    if (numtileC > 0x7fffffffLL) return spg_fail(h, SPG_ERR_INVALID, "C has more than 2^31-1 tiles");
-    C->numtileC = numtileC;
+    SPG_TRY(read_tiles_and_pairs(h, ptr64 + tilem, pairs_total, C, &numtileC));
     SPG_TRY(spg_alloc_t(h, &C->tile_ptrC, (size_t)tilem + 1));
     i64_to_i32_kernel<<<grid_cap(h, tilem + 1, 256, 8), 256, 0, h->stream>>>(ptr64, C->tile_ptrC, tilem + 1);
     SPG_LAUNCHED(h);

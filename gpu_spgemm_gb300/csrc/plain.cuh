@@ -4,6 +4,10 @@
 
 // Per-C private state of the plain path: the matched-pair cache of step 2
 // (spec_* in src/spgemm_raw_v2.cu:161-172) and two device counters.
+// Pairs the step-2 cache holds per C tile (the reference's MAX_MATCHED);
+// a tile with more intersects its lists again in step 3.
+constexpr int SPEC_PAIRS_MAX = 32;
+
 struct PlainPriv {
     int* spec_cnt = nullptr;   // numtileC: cached pair count, -1 = not cached
     int* spec_off = nullptr;   // numtileC

@@ -9,6 +9,7 @@
 // status codes.
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -280,6 +281,23 @@ static bool cache_fits(spg_handle_t h, size_t bytes) {
     return bytes < fr / 4;
 }
 
+// Pair-cache capacity for step 2 over nt C tiles: the cache holds at most
+// SPEC_PAIRS_MAX pairs a tile and, in all, no more than the tile pairs step 1
+// counted (C->pairs), so with that capacity it never overflows.  Where that
+// does not fit beside C, the reference's 8 a tile (src/spgemm_raw_v2.cu:170)
+// with its overflow re-run; 0 when neither fits (no cache: step 3
+// intersects the tile lists again).
+static int64_t spec_capacity(spg_handle_t h, const spg_ctiles* C, int64_t nt) {
+    int64_t cap = std::min<int64_t>(C->pairs, (int64_t)SPEC_PAIRS_MAX * nt);
+    if (const char* d = getenv("SPG_SPEC_CAP_DIV")) {  // test knob: force the overflow re-run
+        const long div = atol(d);
+        if (div > 1) return std::max<int64_t>(1, std::min<int64_t>(cap, 8 * nt) / div);
+    }
+    if (cap > 0 && cache_fits(h, (size_t)cap * 8 + (size_t)C->numtileC * 8)) return cap;
+    cap = 8 * nt;
+    return cap > 0 && cache_fits(h, (size_t)cap * 8 + (size_t)C->numtileC * 8) ? cap : 0;
+}
+
 static float elapsed(spg_handle_t h, int a, int b) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]);
@@ -454,8 +472,8 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         // pair cache covers the listed tiles; every other tile reads "not
         // cached" (-1) and intersects its lists if a plain kernel meets it.
         SPG_TRY(rowwise_symbolic(h, A, B, C, &cp->rw, C->tile_nnzC, cp->rowbin));
-        const int64_t cap = 8 * cp->nplain;
-        if (cache_fits(h, (size_t)cap * 8 + (size_t)nt * 8)) {
+        const int64_t cap = spec_capacity(h, C, cp->nplain);
+        if (cap > 0) {
             cp->plain.spec_cap = cap;
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_cnt, (size_t)nt + 1));
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_off, (size_t)nt + 1));
@@ -467,12 +485,8 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         SPG_TRY(spg_scan_i64_to_i64(h, C->tile_nnzC, C->tile_nnzC, nt));
     } else {
         SPG_TRY(spg_alloc_t(h, &tile_cnt, (size_t)nt + 1));
-        int64_t cap = 8 * nt;  // src/spgemm_raw_v2.cu:170
-        if (const char* d = getenv("SPG_SPEC_CAP_DIV")) {  // test knob: force the overflow re-run
-            const long div = atol(d);
-            if (div > 1) cap = cap / div > 0 ? cap / div : 1;
-        }
-        if (cap > 0 && cache_fits(h, (size_t)cap * 8 + (size_t)nt * 8)) {
+        const int64_t cap = spec_capacity(h, C, nt);
+        if (cap > 0) {
             cp->plain.spec_cap = cap;
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_cnt, (size_t)nt + 1));
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_off, (size_t)nt + 1));
