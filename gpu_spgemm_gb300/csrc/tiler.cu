@@ -87,6 +87,20 @@ __device__ __forceinline__ int narrow_wlo(int r0, int r1, const int* __restrict_
     return max(lo, 0) >> 9;
 }
 
+// A narrow tile-row's nonzeros are one contiguous CSR range: its warp takes
+// them 32 at a time, each lane finding its nonzero's row among the tile-row's
+// row pointers (srp, rows + 1 entries in shared memory): the last q with
+// srp[q] <= j (an empty row shares its pointer with the next one, and the
+// search lands past it).  Walking the 16 rows one after another left most
+// lanes idle on short rows (a 7-point stencil row has 7 nonzeros).
+__device__ __forceinline__ int narrow_row(const int* srp, int nrows, int j) {
+    int q = 0;
+#pragma unroll
+    for (int b = 8; b > 0; b >>= 1)
+        if (q + b < nrows && srp[q + b] <= j) q += b;
+    return q;
+}
+
 // One warp per narrow tile-row: its tile columns in a per-warp bitmap of
 // TL_NARROW_WORDS words (validating canonical CSR on the way), the count.
 __global__ void __launch_bounds__(TL_THREADS)
@@ -94,30 +108,31 @@ tiler_count_narrow_kernel(int m, int n, const int* __restrict__ rp, const int* _
                           const int* __restrict__ rows, const int* __restrict__ n_rows, int* __restrict__ tile_cnt,
                           unsigned* flags) {
     __shared__ uint32_t s_bm[TL_WARPS][TL_NARROW_WORDS];
+    __shared__ int s_rp[TL_WARPS][TS + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* bm = s_bm[warp];
+    int* srp = s_rp[warp];
     const int nr = *n_rows;
     for (int idx = blockIdx.x * TL_WARPS + warp; idx < nr; idx += gridDim.x * TL_WARPS) {
         const int i = rows[idx];
-        const int r0 = i * TS, r1 = min(r0 + TS, m);
+        const int r0 = i * TS, r1 = min(r0 + TS, m), nrows = r1 - r0;
         const int wlo = narrow_wlo(r0, r1, rp, ci);
+        if (lane <= nrows) srp[lane] = rp[r0 + lane];
         for (int w = lane; w < TL_NARROW_WORDS; w += 32) bm[w] = 0u;
         __syncwarp();
-        for (int r = r0; r < r1; r++) {
-            const int s = rp[r], e = rp[r + 1];
-            for (int j = s + lane; j < e; j += 32) {
-                const int c = ci[j];
-                const int prev = (j > s) ? ci[j - 1] : -1;
-                if (c < 0 || c >= n || (j > s && prev >= c)) {
-                    atomicOr(flags, DERR_NONCANONICAL);
-                    continue;
-                }
-                const int tc = c >> 4;
-                if (j > s && (prev >> 4) == tc) continue;  // segment already marked
-                const int w = (tc >> 5) - wlo;
-                if (w < 0 || w >= TL_NARROW_WORDS) { atomicOr(flags, DERR_NONCANONICAL); continue; }
-                atomicOr(&bm[w], 1u << (tc & 31));
+        for (int j = srp[0] + lane; j < srp[nrows]; j += 32) {
+            const int s = srp[narrow_row(srp, nrows, j)];
+            const int c = ci[j];
+            const int prev = (j > s) ? ci[j - 1] : -1;
+            if (c < 0 || c >= n || (j > s && prev >= c)) {
+                atomicOr(flags, DERR_NONCANONICAL);
+                continue;
             }
+            const int tc = c >> 4;
+            if (j > s && (prev >> 4) == tc) continue;  // segment already marked
+            const int w = (tc >> 5) - wlo;
+            if (w < 0 || w >= TL_NARROW_WORDS) { atomicOr(flags, DERR_NONCANONICAL); continue; }
+            atomicOr(&bm[w], 1u << (tc & 31));
         }
         __syncwarp();
         int cnt = 0;
@@ -139,24 +154,25 @@ tiler_fill_narrow_kernel(int m, const int* __restrict__ rp, const int* __restric
                          int* __restrict__ tmp_t, uint8_t* __restrict__ tmp_rp) {
     __shared__ uint32_t s_bm[TL_WARPS][TL_NARROW_WORDS];
     __shared__ uint32_t s_pre[TL_WARPS][TL_NARROW_WORDS];
+    __shared__ int s_rp[TL_WARPS][TS + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* bm = s_bm[warp];
     uint32_t* pre = s_pre[warp];
+    int* srp = s_rp[warp];
     constexpr int WPL = TL_NARROW_WORDS / 32;  // words per lane, contiguous
     const int nr = *n_rows;
     for (int idx = blockIdx.x * TL_WARPS + warp; idx < nr; idx += gridDim.x * TL_WARPS) {
         const int i = rows[idx];
-        const int r0 = i * TS, r1 = min(r0 + TS, m);
+        const int r0 = i * TS, r1 = min(r0 + TS, m), nrows = r1 - r0;
         const int wlo = narrow_wlo(r0, r1, rp, ci);
+        if (lane <= nrows) srp[lane] = rp[r0 + lane];
         for (int w = lane; w < TL_NARROW_WORDS; w += 32) bm[w] = 0u;
         __syncwarp();
-        for (int r = r0; r < r1; r++) {
-            const int s = rp[r], e = rp[r + 1];
-            for (int j = s + lane; j < e; j += 32) {
-                const int tc = ci[j] >> 4;
-                if (j > s && (ci[j - 1] >> 4) == tc) continue;
-                atomicOr(&bm[(tc >> 5) - wlo], 1u << (tc & 31));
-            }
+        for (int j = srp[0] + lane; j < srp[nrows]; j += 32) {
+            const int s = srp[narrow_row(srp, nrows, j)];
+            const int tc = ci[j] >> 4;
+            if (j > s && (ci[j - 1] >> 4) == tc) continue;
+            atomicOr(&bm[(tc >> 5) - wlo], 1u << (tc & 31));
         }
         __syncwarp();
         // exclusive popcount prefix of the words, WPL contiguous words a lane
@@ -182,26 +198,25 @@ tiler_fill_narrow_kernel(int m, const int* __restrict__ rp, const int* __restric
             }
         }
         __syncwarp();
-        for (int r = r0; r < r1; r++) {
-            const int s = rp[r], e = rp[r + 1], rl = r - r0;
-            for (int j = s + lane; j < e; j += 32) {
-                const int c = ci[j], tc = c >> 4;
-                const int w = (tc >> 5) - wlo;
-                const int t = tbase + (int)pre[w] + __popc(bm[w] & ((1u << (tc & 31)) - 1u));
-                int p = 0;
-                for (int q = j - 1; q >= s && (ci[q] >> 4) == tc; q--) p++;
-                tmp_t[j] = t;
-                tmp_rp[j] = (uint8_t)((rl << 4) | p);
-                if (p == 0) {
-                    int len = 1;
-                    uint16_t mk = colbit(c);
-                    for (int q = j + 1; q < e && (ci[q] >> 4) == tc; q++) {
-                        len++;
-                        mk |= colbit(ci[q]);
-                    }
-                    row_cnt[(int64_t)t * TS + rl] = (uint8_t)len;
-                    mask[(int64_t)t * TS + rl] = mk;
+        for (int j = srp[0] + lane; j < srp[nrows]; j += 32) {
+            const int rl = narrow_row(srp, nrows, j);
+            const int s = srp[rl], e = srp[rl + 1];
+            const int c = ci[j], tc = c >> 4;
+            const int w = (tc >> 5) - wlo;
+            const int t = tbase + (int)pre[w] + __popc(bm[w] & ((1u << (tc & 31)) - 1u));
+            int p = 0;
+            for (int q = j - 1; q >= s && (ci[q] >> 4) == tc; q--) p++;
+            tmp_t[j] = t;
+            tmp_rp[j] = (uint8_t)((rl << 4) | p);
+            if (p == 0) {
+                int len = 1;
+                uint16_t mk = colbit(c);
+                for (int q = j + 1; q < e && (ci[q] >> 4) == tc; q++) {
+                    len++;
+                    mk |= colbit(ci[q]);
                 }
+                row_cnt[(int64_t)t * TS + rl] = (uint8_t)len;
+                mask[(int64_t)t * TS + rl] = mk;
             }
         }
         __syncwarp();
