@@ -549,7 +549,8 @@ def run_ours(args):
 
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(h, api, a, b, args, flops, stream, small_c=numtileC < E2E_STREAM_MIN_TILES)
+        small = numtileC < E2E_STREAM_MIN_TILES if args.e2e_mode == "auto" else args.e2e_mode == "whole"
+        e2e = measure_e2e(h, api, a, b, args, flops, stream, small_c=small)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -760,6 +761,25 @@ def galerkin_e2e(h, api, w, args, flops, stream):
                 "d2h_bytes_per_step": None}
 
 
+def e2e_tile_inputs(h, a, b, ha, hb, code):
+    """The step's inputs, host CSR -> device tiles: A row-major, B in CSC tile
+    order.  For A*A (b is a) the CSR crosses once: B is tiled from A's device
+    row view, the copy of the CSR that A's tiles keep."""
+    import ctypes as C
+    from gpu_spgemm_gb300 import _lib as L
+    lib = h.lib
+    ta, tb = L.SpgTiles(), L.SpgTiles()
+    h.check(lib.spg_tile_from_csr_host(h.h, a.m, a.n, a.nnz, ha[0][1].ctypes.data, ha[1][1].ctypes.data,
+                                       ha[2][1].ctypes.data, code, L.SPG_LAYOUT_ROW, 0, C.byref(ta)))
+    if b is a:
+        h.check(lib.spg_tile_from_csr(h.h, a.m, a.n, a.nnz, ta.row_ptr, ta.col_idx, ta.row_val, code,
+                                      L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
+    else:
+        h.check(lib.spg_tile_from_csr_host(h.h, b.m, b.n, b.nnz, hb[0][1].ctypes.data, hb[1][1].ctypes.data,
+                                           hb[2][1].ctypes.data, code, L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
+    return ta, tb
+
+
 def e2e_whole(h, api, a, b, args, flops, pin, code, vd, h2d, ha, hb):
     """End to end for a C small enough to copy whole: per step the CSR inputs
     go host->device and are tiled, spg_spgemm runs steps 1-3, and C's result
@@ -771,11 +791,8 @@ def e2e_whole(h, api, a, b, args, flops, pin, code, vd, h2d, ha, hb):
     out = {}
 
     def one():
-        ta, tb, c = L.SpgTiles(), L.SpgTiles(), L.SpgCTiles()
-        h.check(lib.spg_tile_from_csr_host(h.h, a.m, a.n, a.nnz, ha[0][1].ctypes.data, ha[1][1].ctypes.data,
-                                           ha[2][1].ctypes.data, code, L.SPG_LAYOUT_ROW, 0, C.byref(ta)))
-        h.check(lib.spg_tile_from_csr_host(h.h, b.m, b.n, b.nnz, hb[0][1].ctypes.data, hb[1][1].ctypes.data,
-                                           hb[2][1].ctypes.data, code, L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
+        c = L.SpgCTiles()
+        ta, tb = e2e_tile_inputs(h, a, b, ha, hb, code)
         h.check(lib.spg_spgemm(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], api._PRECS[args.prec],
                                C.byref(c)))
         nt, nz = c.numtileC, c.nnzC
@@ -801,7 +818,7 @@ def e2e_whole(h, api, a, b, args, flops, pin, code, vd, h2d, ha, hb):
         dt = (time.perf_counter() - t0) / steps
         return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": dt * 1e3, "steps": steps,
-                "path": "spg_tile_from_csr_host x2 + spg_spgemm + spg_ctiles_to_host of tile_ptrC, tile_rowidxC, "
+                "path": "spg_tile_from_csr_host (A, and B unless B is A) + spg_tile_from_csr of B from A's row view when B is A + spg_spgemm + spg_ctiles_to_host of tile_ptrC, tile_rowidxC, "
                         "tile_colidxC, tile_nnzC, tile_valC, tile_colC into pinned host buffers"}
     except Exception as e:  # report instead of dying
         return {"value": None, "unit": "GFLOP/s", "error": str(e)[:200], "h2d_bytes_per_step": h2d,
@@ -839,11 +856,11 @@ def measure_e2e(h, api, a, b, args, flops, stream, small_c=False):
         return t, t.numpy()
 
     ha = [pin(a.row_ptr), pin(a.col_idx), pin(a.val)]
-    hb = [pin(b.row_ptr), pin(b.col_idx), pin(b.val)]
+    hb = ha if b is a else [pin(b.row_ptr), pin(b.col_idx), pin(b.val)]
     code = L.SPG_F64 if a.val.dtype == np.float64 else L.SPG_F32
     vd = np.float64 if code == L.SPG_F64 else np.float32
     vsz = np.dtype(vd).itemsize
-    h2d = sum(x[1].nbytes for x in ha + hb)
+    h2d = sum(x[1].nbytes for x in (ha if b is a else ha + hb))
     CT = max(1 << 16, args.e2e_range_tiles)  # C tiles per staged range
     VC = 1 << 27            # values per staged range (ranges halve when a range holds more)
     NW = max(1, args.e2e_copy_workers)
@@ -894,11 +911,8 @@ def measure_e2e(h, api, a, b, args, flops, stream, small_c=False):
         return nb
 
     def one():
-        ta, tb, c = L.SpgTiles(), L.SpgTiles(), L.SpgCTiles()
-        h.check(lib.spg_tile_from_csr_host(h.h, a.m, a.n, a.nnz, ha[0][1].ctypes.data, ha[1][1].ctypes.data,
-                                           ha[2][1].ctypes.data, code, L.SPG_LAYOUT_ROW, 0, C.byref(ta)))
-        h.check(lib.spg_tile_from_csr_host(h.h, b.m, b.n, b.nnz, hb[0][1].ctypes.data, hb[1][1].ctypes.data,
-                                           hb[2][1].ctypes.data, code, L.SPG_LAYOUT_B_CSC, 0, C.byref(tb)))
+        c = L.SpgCTiles()
+        ta, tb = e2e_tile_inputs(h, a, b, ha, hb, code)
         h.check(lib.spg_symbolic_tiles(h.h, C.byref(ta), C.byref(tb), api._ALGOS[args.algo], C.byref(c)))
         tp = np.zeros(c.tilem + 1, np.int32)
         h.check(lib.spg_ctiles_to_host(h.h, C.byref(c), tp.ctypes.data, None, None, None, None, None, None, None))
@@ -989,7 +1003,7 @@ def measure_e2e(h, api, a, b, args, flops, stream, small_c=False):
         return {"value": flops / dt / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": dt * 1e3, "steps": steps,
                 "last_step": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in tstat.items()},
-                "path": "spg_tile_from_csr_host x2 + spg_symbolic_tiles + spg_symbolic_masks + spg_numeric_bands "
+                "path": "spg_tile_from_csr_host (A, and B unless B is A; B tiled from A's device row view when B is A) + spg_symbolic_tiles + spg_symbolic_masks + spg_numeric_bands "
                         "(%d tile-row bands, %s band first); C's result (tile_ptrC, tile_rowidxC, tile_colidxC, tile_nnzC, "
                         "tile_colC, tile_valC, as the reference reads it back) to pinned host staging by "
                         "spg_ctiles_to_host_range on %d copy handles/streams as each part becomes final "
@@ -1098,6 +1112,9 @@ def main():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--e2e-bands", type=int, default=8,
                    help="tile-row bands of the e2e numeric phase (a band's values copy once it is complete)")
+    p.add_argument("--e2e-mode", default="auto", choices=["auto", "stream", "whole"],
+                   help="e2e copy-out: C streamed out band by band while the numeric phase runs, or copied whole "
+                        "after the product (auto: by C's tile count)")
     p.add_argument("--e2e-range-tiles", type=int, default=1 << 23,
                    help="C tiles per staged e2e copy range (pinned staging per copy worker scales with it)")
     p.add_argument("--e2e-band-order", choices=["last", "first"], default="last",
