@@ -14,7 +14,8 @@ struct PlainPriv {
     int* spec_pa = nullptr;    // spec_cap
     int* spec_pb = nullptr;    // spec_cap
     int64_t spec_cap = 0;
-    unsigned long long* counters = nullptr;  // [0] cache allocation, [1] matched pairs (step 2), [2] tile pairs (step 1)
+    unsigned long long* counters = nullptr;  // [0] cache allocation, [1] matched pairs (step 2), [2] tile pairs (step 1),
+                                             // [3] tile pairs of the plain tile-rows of a binned product
 };
 
 spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, spg_ctiles* C,

@@ -32,6 +32,7 @@ struct CPriv {
     int64_t* plain_off = nullptr;  // tilem+1: prefix of the plain tile-rows' C tiles
     int* plain_list = nullptr;     // those C tiles, ascending
     int64_t nplain = 0;
+    int64_t plain_pairs = 0;       // tile pairs of the plain tile-rows (step 1's count)
 };
 
 RowwisePriv* ctiles_rowwise_priv(spg_ctiles* C) {
@@ -281,14 +282,14 @@ static bool cache_fits(spg_handle_t h, size_t bytes) {
     return bytes < fr / 4;
 }
 
-// Pair-cache capacity for step 2 over nt C tiles: the cache holds at most
-// SPEC_PAIRS_MAX pairs a tile and, in all, no more than the tile pairs step 1
-// counted (C->pairs), so with that capacity it never overflows.  Where that
-// does not fit beside C, the reference's 8 a tile (src/spgemm_raw_v2.cu:170)
-// with its overflow re-run; 0 when neither fits (no cache: step 3
-// intersects the tile lists again).
-static int64_t spec_capacity(spg_handle_t h, const spg_ctiles* C, int64_t nt) {
-    int64_t cap = std::min<int64_t>(C->pairs, (int64_t)SPEC_PAIRS_MAX * nt);
+// Pair-cache capacity for step 2 over nt C tiles holding `pairs` tile pairs
+// (step 1's count): the cache holds at most SPEC_PAIRS_MAX pairs a tile and,
+// in all, no more than those pairs, so with that capacity it never
+// overflows.  Where that does not fit beside C, the reference's 8 a tile
+// (src/spgemm_raw_v2.cu:170) with its overflow re-run; 0 when neither fits
+// (no cache: step 3 intersects the tile lists again).
+static int64_t spec_capacity(spg_handle_t h, const spg_ctiles* C, int64_t nt, int64_t pairs) {
+    int64_t cap = std::min<int64_t>(pairs, (int64_t)SPEC_PAIRS_MAX * nt);
     if (const char* d = getenv("SPG_SPEC_CAP_DIV")) {  // test knob: force the overflow re-run
         const long div = atol(d);
         if (div > 1) return std::max<int64_t>(1, std::min<int64_t>(cap, 8 * nt) / div);
@@ -325,10 +326,18 @@ extern "C" spg_status spg_ctiles_free(spg_handle_t h, spg_ctiles* C) {
 // ---------------------------------------------------------------------------
 // SPG_ALGO_BINNED: the C tiles of the tile-rows binned to the plain kernels
 // ---------------------------------------------------------------------------
+// Per tile-row: its C tiles if it is binned plain (else 0); the plain
+// tile-rows' tile pairs summed into *plain_pairs (the pair cache's bound).
 __global__ void plain_count_kernel(int tilem, const uint8_t* __restrict__ rowbin, const int* __restrict__ tile_ptrC,
-                                   int* __restrict__ cnt) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x)
+                                   const int64_t* __restrict__ row_pairs, int* __restrict__ cnt,
+                                   unsigned long long* __restrict__ plain_pairs) {
+    unsigned long long p = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tilem; i += gridDim.x * blockDim.x) {
         cnt[i] = rowbin[i] ? tile_ptrC[i + 1] - tile_ptrC[i] : 0;
+        if (rowbin[i]) p += (unsigned long long)row_pairs[i];
+    }
+    p = warp_sum(p);
+    if ((threadIdx.x & 31) == 0 && p) atomicAdd(plain_pairs, p);
 }
 
 __global__ void plain_list_kernel(int tilem, const uint8_t* __restrict__ rowbin, const int* __restrict__ tile_ptrC,
@@ -356,12 +365,21 @@ static spg_status bin_tiles(spg_handle_t h, spg_ctiles* C, CPriv* cp, spg_algo* 
     int* cnt = nullptr;
     SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
     SPG_TRY(spg_alloc_t(h, &cp->plain_off, (size_t)tilem + 1));
+    unsigned long long* plain_pairs = cp->plain.counters + 3;
+    SPG_CUDA(h, cudaMemsetAsync(plain_pairs, 0, sizeof(unsigned long long), h->stream));
     if (tilem > 0) {
-        plain_count_kernel<<<small_grid(h, tilem, 256), 256, 0, h->stream>>>(tilem, cp->rowbin, C->tile_ptrC, cnt);
+        plain_count_kernel<<<small_grid(h, tilem, 256), 256, 0, h->stream>>>(tilem, cp->rowbin, C->tile_ptrC,
+                                                                             cp->row_pairs, cnt, plain_pairs);
         SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, cp->plain_off, tilem));
-    SPG_TRY(spg_read_i64(h, cp->plain_off + tilem, &cp->nplain));
+    {
+        const int64_t* src[2] = {cp->plain_off + tilem, reinterpret_cast<const int64_t*>(plain_pairs)};
+        int64_t v[2] = {0, 0};
+        SPG_TRY(spg_read_i64s_checked(h, 2, src, v, "binning"));
+        cp->nplain = v[0];
+        cp->plain_pairs = v[1];
+    }
     if (cp->nplain == 0 || cp->nplain == C->numtileC) {
         *algo = cp->nplain == 0 ? SPG_ALGO_ROWWISE : SPG_ALGO_PLAIN;
         spg_free_async(h, cp->rowbin);
@@ -472,7 +490,7 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         // pair cache covers the listed tiles; every other tile reads "not
         // cached" (-1) and intersects its lists if a plain kernel meets it.
         SPG_TRY(rowwise_symbolic(h, A, B, C, &cp->rw, C->tile_nnzC, cp->rowbin));
-        const int64_t cap = spec_capacity(h, C, cp->nplain);
+        const int64_t cap = spec_capacity(h, C, cp->nplain, cp->plain_pairs);
         if (cap > 0) {
             cp->plain.spec_cap = cap;
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_cnt, (size_t)nt + 1));
@@ -485,7 +503,7 @@ static spg_status masks_impl(spg_handle_t h, const spg_tiles* A, const spg_tiles
         SPG_TRY(spg_scan_i64_to_i64(h, C->tile_nnzC, C->tile_nnzC, nt));
     } else {
         SPG_TRY(spg_alloc_t(h, &tile_cnt, (size_t)nt + 1));
-        const int64_t cap = spec_capacity(h, C, nt);
+        const int64_t cap = spec_capacity(h, C, nt, C->pairs);
         if (cap > 0) {
             cp->plain.spec_cap = cap;
             SPG_TRY(spg_alloc_t(h, &cp->plain.spec_cnt, (size_t)nt + 1));
