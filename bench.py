@@ -1054,7 +1054,13 @@ def run_batch(args):
             api.spgemm(h, A, B, algo="plain").free()
     ms_plain = timed(per_product, max(1, args.steps // 2))
     del tiles
-    # (2) batched, autotuned bins
+    # (2) batched, autotuned bins; each bin is one block-diagonal product of
+    # far more than 65,536 A tiles, so the learned step 1 is attached as for a
+    # single large product (one bitmap pass instead of two)
+    sizing = None
+    if args.sizing and os.path.exists(api.SIZING_MODEL_PATH):
+        sizing = api.SizingModel.load(h)
+        sizing.attach(args.sizing_margin)
     bt = api.Batch(h, pairs)
     thr, algos = bt.tune()
     clocks = ClockSampler(local)
@@ -1063,6 +1069,11 @@ def run_batch(args):
     ms_batch = timed(lambda: bt.spgemm(), args.steps)
     launches = (h.launches() - l0) * args.steps // (args.steps + args.warmup)
     clk = clocks.stop()
+    ms_batch_nosz = None
+    if sizing is not None and not args.no_compare:
+        sizing.detach()
+        ms_batch_nosz = timed(lambda: bt.spgemm(), args.steps)
+        sizing.attach(args.sizing_margin)
     # (3) numeric-only graph replay with new values (same structure)
     nz = bt.bins()
     outs = [torch.empty(max(1, int(z)), dtype=torch.float32).pin_memory().numpy() for z in nz]
@@ -1080,7 +1091,11 @@ def run_batch(args):
             "config": {"workload": f"batch of {count} C=A*B, n log-uniform [1024,65536], Erdos-Renyi deg U[4,32], "
                                    "FP32 U[-1,1]", "products": flops / 2},
             "details": {"tuned_thresholds": thr, "tuned_algos": algos,
-                        "graph_numeric_ms": ms_graph, "graph_numeric_gflops": flops / (ms_graph * 1e-3) / 1e9},
+                        "graph_numeric_ms": ms_graph, "graph_numeric_gflops": flops / (ms_graph * 1e-3) / 1e9,
+                        "learned_sizing": "attached (margin %g)" % args.sizing_margin if sizing is not None
+                        else "not attached",
+                        "gflops_without_sizing_model": (flops / (ms_batch_nosz * 1e-3) / 1e9
+                                                        if ms_batch_nosz else None)},
             "vs_plain": {"plain": {"ms_step": ms_plain, "gflops": flops / (ms_plain * 1e-3) / 1e9,
                                    "what": "one plain launch sequence per product"},
                          "speedup_vs_plain": ms_plain / ms_batch},
@@ -1091,6 +1106,9 @@ def run_batch(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     bt.free()
+    if sizing is not None:
+        sizing.detach()
+        sizing.free()
     h.close()
 
 

@@ -22,37 +22,73 @@ constexpr int SPEC_MAX = SPEC_PAIRS_MAX;  // pairs cached per C tile (MAX_MATCHE
 // of the B tile-rows it reaches; B's tile-rows are sorted), so clearing and
 // scanning cost O(span / 32) rather than O(tilenB / 32): a block-diagonal
 // batch of many small products stays cheap.  Word w of the bitmap holds
-// columns 32*(wlo + w) ... ; *s_span receives {wlo, nwd}.  Returns the tile
-// pairs visited (lane 0 partials).
+// columns 32*(wlo + w) ... ; *s_span receives {wlo, nwd}.  Returns the
+// tile-row's tile pairs (thread 0; 0 elsewhere).
+// Saturation: with occ (B's occupied tile columns, exclusive prefix over
+// tilenB + 1) a tile-row whose tile pairs are at least 4x the occupied B
+// columns of its span stops probing once every one of them is set -- no
+// further pair can add a column.  Each warp counts the bitmap after probing
+// 32x as many pairs as it has words, at most four times a row (the counts
+// cost a row that never fills a few percent of its probing at most).  An Erdos-Renyi tile-row (one nonzero
+// a tile) pairs each A tile with all of B's tile-row and fills its span long
+// before its last pair.
 __device__ int64_t build_c_bitmap(int i, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
                                   const int* __restrict__ b_tp, const int* __restrict__ b_tc, uint32_t* bm,
-                                  int* s_span) {
+                                  int* s_span, const int* __restrict__ occ) {
+    __shared__ unsigned long long s_pairs;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int as = a_tp[i], ae = a_tp[i + 1];
-    if (threadIdx.x == 0) { s_span[0] = 0x7fffffff; s_span[1] = -1; }
+    if (threadIdx.x == 0) { s_span[0] = 0x7fffffff; s_span[1] = -1; s_pairs = 0ull; }
     __syncthreads();
     int lo = 0x7fffffff, hi = -1;
+    unsigned long long pp = 0;
     for (int a = as + threadIdx.x; a < ae; a += C1_THREADS) {
         const int k = __ldg(&a_tc[a]);
         const int bs = __ldg(&b_tp[k]), be = __ldg(&b_tp[k + 1]);
+        pp += (unsigned long long)(be - bs);
         if (be > bs) {
             lo = min(lo, __ldg(&b_tc[bs]));
             hi = max(hi, __ldg(&b_tc[be - 1]));
         }
     }
     if (hi >= 0) { atomicMin(&s_span[0], lo); atomicMax(&s_span[1], hi); }
+    pp = warp_sum(pp);
+    if (lane == 0 && pp) atomicAdd(&s_pairs, pp);
     __syncthreads();
     const int jlo = s_span[0], jhi = s_span[1];
     const int wlo = jhi >= 0 ? (jlo >> 5) : 0;
     const int nwd = jhi >= 0 ? (jhi >> 5) - wlo + 1 : 0;
+    const unsigned long long pairs = s_pairs;
+    const int target = (occ && jhi >= 0) ? __ldg(&occ[jhi + 1]) - __ldg(&occ[jlo]) : 0;
+    const bool sat = target > 0 && pairs >= 4ull * (unsigned long long)target;  // block-uniform
     for (int w = threadIdx.x; w < nwd; w += C1_THREADS) bm[w] = 0u;
     __syncthreads();
     if (threadIdx.x == 0) { s_span[2] = wlo; s_span[3] = nwd; }
-    int64_t pairs = 0;
-    for (int a = as + warp; a < ae; a += C1_WARPS) {
+    int a = as + warp;
+    if (sat) {
+        int64_t since = 0;  // pairs this warp probed since its last count
+        int counts = 4;     // a row still short of full after four counts (a power-law hub) stops counting
+        for (; a < ae && counts > 0; a += C1_WARPS) {
+            if (since >= 32 * (int64_t)nwd) {  // warp-uniform
+                since = 0;
+                counts--;
+                int c = 0;
+                for (int w = lane; w < nwd; w += 32) c += __popc(bm[w]);
+                if (warp_sum(c) >= target) { a = ae; break; }  // bits are only ever added: a full count is final
+            }
+            const int k = __ldg(&a_tc[a]);
+            const int bs = __ldg(&b_tp[k]), be = __ldg(&b_tp[k + 1]);
+            since += be - bs;
+            for (int b = bs + lane; b < be; b += 32) {
+                const int j = __ldg(&b_tc[b]) - (wlo << 5);
+                const uint32_t bit = 1u << (j & 31);
+                if (!(bm[j >> 5] & bit)) atomicOr(&bm[j >> 5], bit);
+            }
+        }
+    }
+    for (; a < ae; a += C1_WARPS) {  // every pair (after the counts, for a row that did not fill)
         const int k = __ldg(&a_tc[a]);
         const int bs = __ldg(&b_tp[k]), be = __ldg(&b_tp[k + 1]);
-        pairs += be - bs;
         for (int b = bs + lane; b < be; b += 32) {
             const int j = __ldg(&b_tc[b]) - (wlo << 5);
             const uint32_t bit = 1u << (j & 31);
@@ -60,13 +96,14 @@ __device__ int64_t build_c_bitmap(int i, const int* __restrict__ a_tp, const int
         }
     }
     __syncthreads();
-    return lane == 0 ? pairs : 0;
+    return threadIdx.x == 0 ? (int64_t)pairs : 0;
 }
 
 __global__ void __launch_bounds__(C1_THREADS)
 c1_count_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
                 const int* __restrict__ b_tp, const int* __restrict__ b_tc, int* __restrict__ cnt,
-                int64_t* __restrict__ row_pairs, unsigned long long* __restrict__ pairs_total) {
+                int64_t* __restrict__ row_pairs, unsigned long long* __restrict__ pairs_total,
+                const int* __restrict__ occ) {
     extern __shared__ uint32_t bm[];
     __shared__ int s_c[C1_WARPS];
     __shared__ int64_t s_p[C1_WARPS];
@@ -77,7 +114,7 @@ c1_count_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict_
         if (threadIdx.x == 0) { cnt[i] = 0; row_pairs[i] = 0; }
         return;
     }
-    int64_t pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
+    int64_t pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span, occ);
     const int nwd = s_span[3];
     int c = 0;
     for (int w = threadIdx.x; w < nwd; w += C1_THREADS) c += __popc(bm[w]);
@@ -100,14 +137,14 @@ __global__ void __launch_bounds__(C1_THREADS)
 c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__ a_tc,
                const int* __restrict__ b_tp, const int* __restrict__ b_tc,
                const int* __restrict__ tile_ptrC, int* __restrict__ rowidxC, int* __restrict__ colidxC,
-               const int* __restrict__ rows) {
+               const int* __restrict__ rows, const int* __restrict__ occ) {
     extern __shared__ uint32_t bm[];
     __shared__ int64_t s_sh[C1_WARPS + 1];
     __shared__ int s_span[4];
     const int i = rows ? rows[blockIdx.x] : (int)blockIdx.x;
     (void)nwords;
     if (tile_ptrC[i] == tile_ptrC[i + 1]) return;
-    build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
+    build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span, occ);
     const int wlo = s_span[2], nwd = s_span[3];
     const int wpt = (nwd + C1_THREADS - 1) / C1_THREADS;
     const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
@@ -137,7 +174,8 @@ c1_fill_kernel(int nwords, const int* __restrict__ a_tp, const int* __restrict__
 __global__ void __launch_bounds__(C1_THREADS)
 c1_slot_kernel(const int* __restrict__ a_tp, const int* __restrict__ a_tc, const int* __restrict__ b_tp,
                const int* __restrict__ b_tc, const int64_t* __restrict__ slot_off, int* __restrict__ slot_col,
-               int* __restrict__ cnt, int64_t* __restrict__ row_pairs, unsigned long long* __restrict__ pairs_total) {
+               int* __restrict__ cnt, int64_t* __restrict__ row_pairs, unsigned long long* __restrict__ pairs_total,
+               const int* __restrict__ occ) {
     extern __shared__ uint32_t bm[];
     __shared__ int s_span[4];
     __shared__ int64_t s_sh[C1_WARPS + 1];
@@ -147,7 +185,7 @@ c1_slot_kernel(const int* __restrict__ a_tp, const int* __restrict__ a_tc, const
         if (threadIdx.x == 0) { cnt[i] = 0; row_pairs[i] = 0; }
         return;
     }
-    int64_t pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span);
+    int64_t pairs = build_c_bitmap(i, a_tp, a_tc, b_tp, b_tc, bm, s_span, occ);
     const int wlo = s_span[2], nwd = s_span[3];
     const int wpt = (nwd + C1_THREADS - 1) / C1_THREADS;
     const int w0 = min(nwd, (int)threadIdx.x * wpt), w1 = min(nwd, w0 + wpt);
@@ -198,6 +236,13 @@ __global__ void c1_compact_kernel(int tilem, const int* __restrict__ tile_ptrC, 
             __stcs(&rowidxC[t0 + k], i);
         }
     }
+}
+
+// occ[j] = 1 where B's tile column j holds a tile (scanned into the prefix
+// build_c_bitmap's saturation exit reads).
+__global__ void occupied_cols_kernel(int tilen, const int* __restrict__ csc_tile_ptr, int* __restrict__ occ) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < tilen; j += gridDim.x * blockDim.x)
+        occ[j] = csc_tile_ptr[j + 1] > csc_tile_ptr[j] ? 1 : 0;
 }
 
 __device__ __forceinline__ int lower_bound_dev(const int* __restrict__ a, int lo, int hi, int key) {
@@ -716,6 +761,25 @@ __global__ void i64_to_i32_kernel(const int64_t* __restrict__ in, int* __restric
         out[t] = (int)in[t];
 }
 
+int grid_cap(spg_handle_t h, int64_t units, int per_block, int per_sm) {
+    int64_t g = ceil_div(units, per_block);
+    const int64_t cap = (int64_t)h->num_sms * per_sm;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// B's occupied tile columns as an exclusive prefix (tilen + 1 entries), for
+// step 1's saturation exit; built for products of at least 65,536 A tiles
+// (two launches are noise there), null below.
+spg_status occupied_prefix(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, ScratchList& sc, int** occ) {
+    *occ = nullptr;
+    if (A->numtile < 65536 || B->tilen <= 0 || !B->csc_tile_ptr) return SPG_OK;
+    SPG_TRY(sc.alloc(occ, (size_t)B->tilen + 1));
+    occupied_cols_kernel<<<grid_cap(h, B->tilen, 256, 8), 256, 0, h->stream>>>(B->tilen, B->csc_tile_ptr, *occ);
+    SPG_LAUNCHED(h);
+    return spg_scan_i32_to_i32(h, *occ, *occ, B->tilen);
+}
+
 // C's tile count and step 1's tile pairs (C->pairs) in one round trip,
 // with step 1's device errors.
 spg_status read_tiles_and_pairs(spg_handle_t h, const int64_t* d_numtile, const unsigned long long* pairs_total,
@@ -730,12 +794,7 @@ spg_status read_tiles_and_pairs(spg_handle_t h, const int64_t* d_numtile, const 
     return SPG_OK;
 }
 
-int grid_cap(spg_handle_t h, int64_t units, int per_block, int per_sm) {
-    int64_t g = ceil_div(units, per_block);
-    const int64_t cap = (int64_t)h->num_sms * per_sm;
-    if (g > cap) g = cap;
-    return (int)(g < 1 ? 1 : g);
-}
+
 
 }  // namespace
 
@@ -751,12 +810,14 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     ScratchList sc(h);
     int* cnt = nullptr;
     int64_t* ptr64 = nullptr;
+    int* occ = nullptr;
     SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
     SPG_TRY(sc.alloc(&ptr64, (size_t)tilem + 1));
+    SPG_TRY(occupied_prefix(h, A, B, sc, &occ));
     if (tilem > 0) {
         c1_count_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx,
                                                                B->tile_ptr, B->tile_columnidx, cnt, row_pairs,
-                                                               pairs_total);
+                                                               pairs_total, occ);
         SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
@@ -770,7 +831,7 @@ spg_status plain_step1(spg_handle_t h, const spg_tiles* A, const spg_tiles* B, s
     if (tilem > 0 && numtileC > 0) {
         c1_fill_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                               B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
-                                                              C->tile_colidxC, nullptr);
+                                                              C->tile_colidxC, nullptr, occ);
         SPG_LAUNCHED(h);
     }
     return SPG_OK;
@@ -807,13 +868,15 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
     int* slot_col = nullptr;
     int* cnt = nullptr;
     int64_t* ptr64 = nullptr;
+    int* occ = nullptr;
     SPG_TRY(spg_workspace(h, SPG_WS_SLOTS, sizeof(int) * ((size_t)cap + 1), reinterpret_cast<void**>(&slot_col)));
     SPG_TRY(sc.alloc(&cnt, (size_t)tilem + 1));
     SPG_TRY(sc.alloc(&ptr64, (size_t)tilem + 1));
+    SPG_TRY(occupied_prefix(h, A, B, sc, &occ));
     if (tilem > 0) {
         c1_slot_kernel<<<tilem, C1_THREADS, smem, h->stream>>>(A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                               B->tile_columnidx, slot_off, slot_col, cnt, row_pairs,
-                                                              pairs_total);
+                                                              pairs_total, occ);
         SPG_LAUNCHED(h);
     }
     SPG_TRY(spg_scan_i32_to_i64(h, cnt, ptr64, tilem));
@@ -837,7 +900,7 @@ spg_status plain_step1_sized(spg_handle_t h, const spg_tiles* A, const spg_tiles
             h->stats.overflow_reruns += nov;
             c1_fill_kernel<<<nov, C1_THREADS, smem, h->stream>>>(nwords, A->tile_ptr, A->tile_columnidx, B->tile_ptr,
                                                                 B->tile_columnidx, C->tile_ptrC, C->tile_rowidxC,
-                                                                C->tile_colidxC, over_rows);
+                                                                C->tile_colidxC, over_rows, occ);
             SPG_LAUNCHED(h);
         }
     }
