@@ -141,6 +141,30 @@ def test_rowwise_numeric_after_plain_symbolic(handle, dtype):
         Cm.free()
 
 
+@pytest.mark.parametrize("sizing", [False, True], ids=["exact-two-pass", "learned-sizing"])
+def test_step1_saturation_exit_er(handle, sizing):
+    """Erdos-Renyi 32,768 x 32,768, degree 16 (493,562 A tiles, one nonzero
+    a tile): every C tile-row holds all 2,048 tile columns, which its tile
+    pairs (about 57,000 a row) reach long before the last one, so step 1
+    stops probing early.  C's tile set, tile pairs and the rest of the
+    structure still equal the oracle's full step 1."""
+    if sizing and not os.path.exists(api.SIZING_MODEL_PATH):
+        pytest.skip("no trained sizing model shipped")
+    rng = np.random.Generator(np.random.PCG64(7))
+    a = synth.erdos_renyi(32768, 16.0, rng)
+    model = None
+    if sizing:
+        model = api.SizingModel.load(handle)
+        model.attach(1.0)
+    try:
+        got, S = check_product(handle, a, a, "rowwise", np.float32)
+    finally:
+        if model is not None:
+            model.detach()
+            model.free()
+    assert got["numtileC"] == 2048 * 2048
+
+
 def test_host_range_copy_matches_full(handle):
     import ctypes as C
     from gpu_spgemm_gb300 import _lib as L
